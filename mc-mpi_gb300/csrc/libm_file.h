@@ -1,0 +1,57 @@
+/*
+ * libm_file.h - on-disk layout of the host-libm exception table written by
+ * libm_tablegen and read by the library when a strict context is created.
+ *
+ *   mcg_libm_file header
+ *   uint32_t log_pairs[2 * n_log]   (argument bits, host logf result bits)
+ *   uint32_t exp_pairs[2 * n_exp]   (argument bits, host expf result bits)
+ *
+ * The fingerprint hashes the host library's logf/expf on a fixed set of
+ * arguments; the loader recomputes it so a table made against another C
+ * library (another machine) is refused instead of silently used.
+ * Host-only header.
+ */
+#ifndef MCG_LIBM_FILE_H
+#define MCG_LIBM_FILE_H
+
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#define MCG_LIBM_MAGIC "MCGLIBM1"
+#ifndef MCG_TAU_BUCKETS
+#define MCG_TAU_BUCKETS 8192
+#endif
+
+typedef struct mcg_libm_file {
+  char magic[8];
+  char libc_version[56];
+  uint64_t fingerprint;
+  uint32_t n_log, n_exp;
+  float tau_log[MCG_TAU_BUCKETS];
+  float tau_exp[MCG_TAU_BUCKETS];
+} mcg_libm_file;
+
+/* FNV-1a over the bits of logf/expf at 8192 arguments spread over both
+ * domains by a 32-bit LCG. */
+static inline uint64_t mcg_libm_fingerprint(void)
+{
+  uint64_t h = 1469598103934665603ull;
+  uint32_t s = 12345u;
+  for (int i = 0; i < 8192; ++i) {
+    s = s * 1664525u + 1013904223u;
+    uint32_t ux = (s >> 2) % 0x3f800000u + 1u; /* (0, 1] */
+    float x, y;
+    memcpy(&x, &ux, 4);
+    y = (i & 1) ? expf(-x * 17.0f) : logf(x);
+    uint32_t uy;
+    memcpy(&uy, &y, 4);
+    for (int b = 0; b < 4; ++b) {
+      h ^= (uy >> (8 * b)) & 0xffu;
+      h *= 1099511628211ull;
+    }
+  }
+  return h;
+}
+
+#endif
