@@ -1,0 +1,327 @@
+#!/usr/bin/env python3
+"""Benchmark of the particle-history hot path on GB300.
+
+Workload (the metric's configuration, "config 1" of the reference's
+headline): slab [0, 1] in 10,000 cells decomposed into 64 contiguous
+sub-domains (decompose_domain, per-layer dx), sigma_a(x) = 0.5 + 0.4 sin(6 pi x),
+sigma_s(x) = 2.0 + 1.5 cos(4 pi x) at cell centres (fp32), particles born at
+x = 0, mu = 1, weight 1.0, seeds from the reference's rnd_seed chain started
+at 5127801, minimum weight 1e-12 (implicit capture, as Layer::simulate).
+The full problem is 1e8 histories; one bench step runs one batch of
+--batch consecutive histories of that source (default 1e7, so 10 steps
+cover the whole 1e8).  Synthetic data: the reference has no dataset.
+
+value : histories/s of the strict tracker with the batch's particles
+        already resident in HBM (mcg_simulate_device), CUDA-event time of
+        the kernel, L2 flushed (256 MB memset) between steps.
+e2e   : histories/s through the C ABI with host buffers (mcg_simulate on
+        pinned host particles: H2D particles, kernel, D2H particles +
+        results + tally), wall time per step.
+--impl reference : the reference's CPU implementation of the path (the
+        oracle port of src/layer.cpp on all host cores), same metric.
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "histories/s on 1 GB300 (plain vs batched vs fwd+adjoint) at matched tally std err"
+NB_CELLS, N_LAYERS, N_TOTAL = 10000, 64, 100_000_000
+BASE_SEED = 5127801
+MIN_W = 1e-12
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p.get("hbm_gbs", 6800.0), "measured"
+    except OSError:
+        return 6800.0, "fallback"
+
+
+def physics(nb=NB_CELLS):
+    xc = (np.arange(nb, dtype=np.float64) + 0.5) / nb
+    sa = (0.5 + 0.4 * np.sin(6 * np.pi * xc)).astype(np.float32)
+    ss = (2.0 + 1.5 * np.cos(4 * np.pi * xc)).astype(np.float32)
+    sigs = (sa + ss).astype(np.float32)
+    rates = (sa / sigs).astype(np.float32)
+    return sigs, rates
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if s[3 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ------------------------------------------------------------------ CPU leg
+def cpu_rate(n_hist, threads, first=0):
+    """Oracle port of Layer::simulate over the decomposed slab on host cores:
+    histories/s on histories first .. first+n_hist-1 of the source."""
+    import oracle as O
+    sigs, rates = physics()
+    layers = list(O.decompose(0.0, 1.0, NB_CELLS, N_LAYERS))
+    p = np.zeros(n_hist, O.PARTICLE_DTYPE)
+    s = O.lcg_skip(BASE_SEED, first, True)
+    p["seed"] = O.rnd_seed_chain(s, n_hist)
+    p["x"], p["mu"], p["wmc"], p["index"] = 0.0, 1.0, 1.0, 0
+    t0 = time.perf_counter()
+    r = O.simulate_histories(layers, sigs, rates, MIN_W, p, 2.0 ** 35, nthreads=threads)
+    dt = time.perf_counter() - t0
+    steps = int(r["traces"]["steps"].sum())
+    return n_hist / dt, steps, dt
+
+
+def cpu_baseline(budget_s=12.0, threads=None):
+    threads = threads or os.cpu_count()
+    rate, steps, dt = cpu_rate(max(threads * 4, 64), threads)
+    n = int(max(threads * 8, min(2_000_000, rate * budget_s)))
+    rate, steps, dt = cpu_rate(n, threads, first=7_000_000)
+    return {"value": rate, "unit": "histories/s", "cores": threads, "kind": "port",
+            "sample": f"{n} histories of the 1e8-history source (indices 7e6..), {steps} steps, "
+                      f"{dt:.1f} s on {threads} threads",
+            "steps_per_s": steps / dt}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count()
+    rate, steps, dt = cpu_rate(max(threads * 4, 64), threads)
+    per_step = int(max(threads * 8, min(2_000_000, rate * 4.0)))
+    times = []
+    for k in range(args.warmup + args.steps):
+        rate, steps, dt = cpu_rate(per_step, threads, first=3_000_000 + k * per_step)
+        if k >= args.warmup:
+            times.append(dt)
+    value = per_step * len(times) / sum(times)
+    line = {
+        "metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": "slab 10000 cells / 64 sub-domains, 1e8 histories from x=0 mu=1",
+                   "batch": per_step, "l2": "n/a (host)"},
+        "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port",
+                         "sample": f"{per_step} histories per step"},
+        "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------ GPU leg
+def run_gpu(args):
+    import torch
+    import importlib.util
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    spec = importlib.util.spec_from_file_location(
+        "mc_mpi_gb300", os.path.join(ROOT, "mc-mpi_gb300", "__init__.py"),
+        submodule_search_locations=[os.path.join(ROOT, "mc-mpi_gb300")])
+    mcg = importlib.util.module_from_spec(spec)
+    sys.modules["mc_mpi_gb300"] = mcg
+    spec.loader.exec_module(mcg)
+
+    B = args.batch
+    sigs, rates = physics()
+    st, m, dx, _, _ = mcg.layer_decomposition(0.0, 1.0, NB_CELLS, N_LAYERS)
+    ctx = mcg.Context(mode=args.mode, device=local)
+    ctx.set_layers(st, m, dx, sigs, rates, MIN_W)
+    ctx.set_tally_scale(35)
+
+    # device-resident particles of the batch: built on the device by the
+    # source kernel before the timed region (histories k*B .. of this rank)
+    part = torch.empty(B * 24, dtype=torch.uint8, device="cuda")
+    res = torch.empty(B, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    host_p = torch.empty(B * 24, dtype=torch.uint8).pin_memory()
+    host_r = torch.empty(B, dtype=torch.int32).pin_memory()
+
+    def batch_first(k):
+        return (rank * (args.warmup + args.steps) + k) * B % N_TOTAL
+
+    def make_batch(k):
+        arr = np.frombuffer(host_p.numpy(), dtype=mcg.PARTICLE_DTYPE)
+        src = mcg.Source(0, 0, BASE_SEED, 0.0, 1.0, 1.0, 0)
+        mcg._check(mcg.load_library().mcg_create_particles(
+            ctx.h, C.byref(src), batch_first(k), B, arr.ctypes.data_as(C.c_void_p)))
+
+    def device_step(k):
+        make_batch(k)
+        part.copy_(host_p, non_blocking=False)
+        flush.zero_()
+        torch.cuda.synchronize()
+        ctx.simulate_device_ptr(part.data_ptr(), B, res.data_ptr())
+        return ctx.last_kernel_ms()
+
+    for k in range(args.warmup):
+        device_step(k)
+    ctx.tally_reset()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    kernel_ms = []
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            kernel_ms.append(device_step(args.warmup + k))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    counters = ctx.counters()
+    dev_s = sum(kernel_ms) / 1e3
+    if dist:
+        t = torch.tensor([dev_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s = float(t.item())
+    value = ws * B * args.steps / dev_s
+
+    # e2e through the C ABI with pinned host buffers
+    lib = mcg.load_library()
+    e2e_times = []
+    for k in range(max(1, min(args.steps, 3)) + 1):
+        make_batch(args.warmup + k)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        mcg._check(lib.mcg_simulate(ctx.h, C.c_void_p(host_p.data_ptr()), B,
+                                    C.c_void_p(host_r.data_ptr()), None, None))
+        tq = ctx.tally_q()
+        e2e_times.append(time.perf_counter() - t1)
+    e2e_s = statistics.median(e2e_times[1:])
+    e2e_val = B / e2e_s
+
+    # roofline of the tracker kernel: algorithmic bytes per launch
+    hbm_peak, peak_kind = peaks()
+    bytes_per_hist = 24 + 24 + 4  # particle in, particle out, result
+    mean_ms = sum(kernel_ms) / len(kernel_ms)
+    achieved = bytes_per_hist * B / (mean_ms / 1e3) / 1e9
+    steps_per_s = counters["steps"] / dev_s if not dist else None
+    clocks = clk.summary()
+    f_sm = (clocks["sm_mhz"] or 1470.0) * 1e6
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    n_alg = 20.0 + 6.0 * counters["scatters"] / max(counters["steps"], 1)
+    issue_frac = (counters["steps"] / dev_s) * n_alg / (sms * 128 * f_sm) if steps_per_s else None
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "slab 10000 cells / 64 sub-domains (decompose_domain), sigma_a="
+                               "0.5+0.4sin(6pi x), sigma_s=2+1.5cos(4pi x), 1e8 histories from "
+                               "x=0 mu=1 w=1, rnd_seed chain 5127801, min weight 1e-12",
+                   "batch": B, "mode": args.mode, "parallelism": f"histories sharded x{ws}",
+                   "l2": "flushed between steps (256 MB memset)"},
+        "steps_per_s": counters["steps"] / dev_s * ws,
+        "collisions_per_s": counters["scatters"] / dev_s * ws,
+        "wall_s": wall,
+        "gpu_launches": args.steps,
+        "e2e": {"value": e2e_val * ws, "unit": "histories/s",
+                "h2d_bytes_per_step": 24 * B, "d2h_bytes_per_step": 28 * B + 8 * NB_CELLS},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "peak_source": peak_kind,
+                     "note": "the tracker is issue-bound; see issue_roofline"},
+        "issue_roofline": {"bound": "issue", "n_alg_ops_per_step": n_alg,
+                           "achieved_gops": (counters["steps"] / dev_s) * n_alg / 1e9,
+                           "peak_gops": sms * 128 * f_sm / 1e9, "frac": issue_frac},
+        "clocks": clocks,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mode", default="strict", choices=["strict", "fast"])
+    ap.add_argument("--batch", type=int, default=10_000_000)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,180 @@
+/*
+ * mcgb300.h - C ABI of the GB300 particle-history tracker (libmcgb300.so).
+ *
+ * Drop-in for the hot path of lkskstlr/mc-mpi: Layer::simulate with its
+ * per-cell weights_absorbed tally (src/layer.cpp:123-361), the GPU seam
+ * cusimulate (include/culayer/culayer.hpp:6-13, src/culayer.cu:41-92) and the
+ * inter-layer particle hand-over of the sync/async/rma workers
+ * (src/worker_sync.cpp:41-120, src/async_comm.cpp, src/rma_comm.cpp).
+ *
+ * Conventions
+ *  - Every function but cusimulate returns an int status (MCG_OK = 0); the
+ *    message of the last failure on the calling thread is mcg_last_error().
+ *  - Pointers named h_* are host memory, d_* device memory of the context's
+ *    GPU; sizes are element counts.
+ *  - A context owns its device buffers and one CUDA stream; calls on one
+ *    context are stream-ordered and synchronous unless named *_async.  A
+ *    context is used by one host thread at a time (like a Layer).
+ *  - Cells are indexed globally (Particle::index).  A context holds one chain
+ *    of contiguous layers; a history ends when its weight drops below the
+ *    minimum (result 0) or it leaves the chain (result -1 left, +1 right).
+ *  - Tallies are 64-bit fixed point: each deposit dw adds llrint(dw * 2^S);
+ *    the sums are exact, so results do not depend on thread order.
+ */
+#ifndef MCGB300_H
+#define MCGB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Particle, byte-compatible with include/types/particle.hpp:7-17 (24 B). */
+typedef struct mcg_particle {
+  uint64_t seed;
+  float x;
+  float mu;
+  float wmc;
+  int32_t index;
+} mcg_particle;
+
+enum mcg_status {
+  MCG_OK = 0,
+  MCG_ERR_ARG = 1,      /* invalid argument */
+  MCG_ERR_CUDA = 2,     /* CUDA runtime error */
+  MCG_ERR_OVERFLOW = 3, /* a hand-over queue or fixed-size buffer overflowed */
+  MCG_ERR_TIMEOUT = 4,  /* a bounded device-side wait gave up */
+  MCG_ERR_STATE = 5,    /* call out of order (no layers set, ...) */
+  MCG_ERR_TABLES = 6,   /* strict mode: host-libm exception table missing or stale */
+  MCG_ERR_LIMIT = 7     /* a history exceeded the step limit */
+};
+
+/* Arithmetic of the step (src/layer.cpp:123-190):
+ *  STRICT: the reference's float operations in the reference's order, no
+ *          contraction, logf/expf bit-identical to the host C library the
+ *          library was built against -> every particle's trajectory, step
+ *          count and final state equal the CPU reference's.
+ *  FAST:   the same physics with hardware log2/exp2, cached reciprocals and
+ *          an accurate 1 - exp; tallies agree statistically. */
+enum mcg_mode { MCG_MODE_STRICT = 0, MCG_MODE_FAST = 1 };
+
+typedef struct mcg_context mcg_context;
+
+const char *mcg_last_error(void);
+const char *mcg_version(void);
+
+/* Create a context on CUDA device `device`.  Strict mode loads the host-libm
+ * exception table built next to the library (or $MCG_LIBM_TABLE). */
+int mcg_create(int device, int mode, mcg_context **out);
+int mcg_destroy(mcg_context *ctx);
+int mcg_set_mode(mcg_context *ctx, int mode);
+
+/* Layers: replaces the Layer constructor / decompose_domain
+ * (src/layer.cpp:17-69).  Layer l covers cells [index_start[l],
+ * index_start[l] + m[l]) with spacing dx[l]; layers must be contiguous.
+ * sigs/rates are per global cell of the chain, first entry = cell
+ * index_start[0] (Layer::sigs, Layer::absorption_rates).  Resets the tally. */
+int mcg_set_layers(mcg_context *ctx, int n_layers, const int32_t *h_index_start,
+                   const int32_t *h_m, const float *h_dx, const float *h_sigs,
+                   const float *h_rates, float particle_min_weight);
+
+/* decompose_domain(x_min, x_max, ., n_layers, r, nb_cells, ., .) for every r,
+ * then mcg_set_layers.  h_sigs/h_rates may be NULL: the constructor's
+ * defaults sigs = expf(-x_mid), rates = 0.5 (src/layer.cpp:54-63). */
+int mcg_set_slab(mcg_context *ctx, float x_min, float x_max, int32_t nb_cells, int32_t n_layers,
+                 const float *h_sigs, const float *h_rates, float particle_min_weight);
+
+/* Fixed-point scale 2^log2_scale of the tally (default 40).  Resets it. */
+int mcg_set_tally_scale(mcg_context *ctx, int32_t log2_scale);
+int mcg_tally_reset(mcg_context *ctx);
+/* Per chain cell: raw fixed-point sums and/or their value as double. */
+int mcg_tally_read(mcg_context *ctx, int64_t *h_q, double *h_f64);
+
+/* Run histories of n host particles (Particle array, updated in place with
+ * the final state).  h_results (may be NULL): -1/0/+1 per particle.
+ * h_steps, h_scatters (may be NULL): particle_step calls and in-cell
+ * scatters per particle.  Host<->device copies included. */
+int mcg_simulate(mcg_context *ctx, mcg_particle *h_particles, int64_t n, int32_t *h_results,
+                 int64_t *h_steps, int64_t *h_scatters);
+
+/* The same on device-resident buffers (no copies); enqueued on the
+ * context's stream and waited for. */
+int mcg_simulate_device(mcg_context *ctx, mcg_particle *d_particles, int64_t n,
+                        int32_t *d_results, int64_t *d_steps, int64_t *d_scatters);
+
+/* Particles born on the device (no particle upload).  Particle i of the
+ * source (i = first .. first+n-1) gets
+ *   seed_mode 0: the (i+1)-th value of the rnd_seed chain started at base_seed
+ *                (src/random.cpp:24-29, as Layer::create_particles draws them)
+ *   seed_mode 1: base_seed + i
+ * then x = x0, index = cell0, wmc = w0, and mu = mu0, or (isotropic != 0)
+ * mu = 2*rnd_real(seed) - 1 as src/layer.cpp:112 (isotropic == 2: mu in
+ * [0,1) via rnd_real).  Only tallies and counters are produced. */
+typedef struct mcg_source {
+  int32_t seed_mode;
+  int32_t isotropic;
+  uint64_t base_seed;
+  float x0, mu0, w0;
+  int32_t cell0;
+} mcg_source;
+int mcg_simulate_source(mcg_context *ctx, const mcg_source *src, int64_t first, int64_t n);
+
+/* Materialise particles first .. first+n-1 of a source into host memory, as
+ * Layer::create_particles does (src/layer.cpp:89-121) for seed_mode 0,
+ * isotropic 1. */
+int mcg_create_particles(mcg_context *ctx, const mcg_source *src, int64_t first, int64_t n,
+                         mcg_particle *h_out);
+
+/* Counters accumulated since the last tally reset. */
+typedef struct mcg_counters {
+  int64_t histories;     /* finished histories */
+  int64_t steps;         /* particle_step calls */
+  int64_t scatters;      /* collisions (in-cell direction changes) */
+  int64_t leaked_left;   /* histories ending with result -1 */
+  int64_t leaked_right;  /* histories ending with result +1 */
+  int64_t killed;        /* histories ending below the minimum weight */
+  int64_t w_left_q;      /* fixed-point weight carried out to the left */
+  int64_t w_right_q;     /* ... to the right */
+  int64_t w_killed_q;    /* ... remaining when killed */
+  int64_t error_flags;   /* nonzero: a bounded wait or limit tripped */
+} mcg_counters;
+int mcg_counters_read(mcg_context *ctx, mcg_counters *out);
+
+/* Timing of the last kernel launch of this context (CUDA events around the
+ * launch on the context's stream), in milliseconds. */
+int mcg_last_kernel_ms(mcg_context *ctx, float *ms);
+
+/* Launch shape (0 = automatic): threads per block, resident blocks per SM,
+ * steps between lane refills. */
+int mcg_set_launch(mcg_context *ctx, int32_t block, int32_t blocks_per_sm, int32_t refill_steps);
+
+/* Longest history, in steps, before the tracker stops it with result 2 and
+ * the call returns MCG_ERR_LIMIT (default 2^28; the reference has none). */
+int mcg_set_step_limit(mcg_context *ctx, int64_t max_steps);
+
+/* Drop-in for the reference GPU seam (include/culayer/culayer.hpp:6-13):
+ * runs particles[0..n) until each leaves [min_index, max_index) (no weight
+ * cut, as the reference kernel), adds the deposits to weights_absorbed[m]
+ * (float, local cell order) and writes every final state back (the reference
+ * lost finished particles, src/culayer.cu:31-32,84-86).  Uses a per-thread
+ * strict context; on failure prints mcg_last_error() and exits like
+ * gpu_errcheck (include/gpu_errcheck/gpu_errcheck.hpp:10-18). */
+void cusimulate(int n, mcg_particle *particles, float const *const sigs,
+                float const *const absorption_rates, float *const weights_absorbed,
+                int min_index, int max_index, float dx);
+/* Same, returning a status instead of exiting. */
+int mcg_cusimulate(int n, mcg_particle *particles, const float *sigs, const float *absorption_rates,
+                   float *weights_absorbed, int min_index, int max_index, float dx);
+
+/* One rnd_real step on n device seeds (src/curandom.cu:7-14). */
+int mcg_rnd_real_device(mcg_context *ctx, uint64_t *d_seeds, float *d_reals, int64_t n);
+
+/* Strict-mode libm on the GPU for n arguments (testing aid): fn 0 logf on
+ * [0, 1], fn 1 expf on [-17.5, 89); other arguments give NaN. */
+int mcg_libm_eval_device(mcg_context *ctx, int fn, const float *d_in, float *d_out, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCGB300_H */

@@ -18,6 +18,7 @@
  *         verified here too.
  *
  * Usage: libm_tablegen <output file>
+ *        libm_tablegen --fingerprint-matches <table>   (exit 0 if current)
  * Build: g++ -O2 -std=c++17 -ffp-contract=off -fopenmp (no -ffast-math).
  */
 #include <algorithm>
@@ -45,6 +46,15 @@ static uint32_t asu(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
 
 int main(int argc, char **argv)
 {
+  if (argc == 3 && strcmp(argv[1], "--fingerprint-matches") == 0) {
+    mcg_libm_file h;
+    FILE *fp = fopen(argv[2], "rb");
+    bool ok = fp && fread(&h, sizeof(h), 1, fp) == 1 && memcmp(h.magic, MCG_LIBM_MAGIC, 8) == 0 &&
+              h.fingerprint == mcg_libm_fingerprint();
+    if (fp)
+      fclose(fp);
+    return ok ? 0 : 1;
+  }
   if (argc != 2) {
     fprintf(stderr, "usage: %s <output file>\n", argv[0]);
     return 2;

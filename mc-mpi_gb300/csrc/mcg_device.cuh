@@ -1,0 +1,170 @@
+/*
+ * mcg_device.cuh - device building blocks of the trackers: the reference's
+ * LCG (src/random.cpp:12-16), the strict libm with its host-libm exception
+ * tables, the fast approximations, and fixed-point tally conversion.
+ */
+#ifndef MCG_DEVICE_CUH
+#define MCG_DEVICE_CUH
+
+#include <cstdint>
+#include <cfloat>
+#include "exact_libm.h"
+
+#define MCG_EPS 1e-4f              /* EPS_PRECISION, include/types/types.hpp:15 */
+#define MCG_MAXREAL FLT_MAX        /* MAXREAL, include/types/types.hpp:14 */
+#define MCG_RNG_G 6364136223846793005ull
+#define MCG_RNG_C 1442695040888963407ull
+#define MCG_RNGS_G 5177284530976225183ull
+#define MCG_RNGS_C 2096348467109453893ull
+#define MCG_MASK63 0x7fffffffffffffffull
+#define MCG_HASH_EMPTY 0xffffffffu
+
+/* Host-libm exception table as seen by kernels (device pointers). */
+struct mcg_libm_dev {
+  const float *tau_log;  /* [MCG_TAU_BUCKETS], -1 where no exception */
+  const float *tau_exp;
+  const uint2 *hash_log; /* open addressing, key = argument bits */
+  const uint2 *hash_exp;
+  uint32_t mask_log, mask_exp;
+  int32_t probes_log, probes_exp; /* longest probe sequence + 1 */
+  float tau_log_max, tau_exp_max;
+};
+
+/* rnd_real: s <- (G s + C) mod 2^63; h = RN((float)s) * 2^-63 */
+__device__ __forceinline__ float mcg_rnd_real(uint64_t &s)
+{
+  s = (MCG_RNG_G * s + MCG_RNG_C) & MCG_MASK63;
+  return __fmul_rn(__ull2float_rn(s), 0x1p-63f);
+}
+
+__device__ __forceinline__ uint64_t mcg_rnd_seed(uint64_t &s)
+{
+  s = (MCG_RNGS_G * s + MCG_RNGS_C) & MCG_MASK63;
+  return s;
+}
+
+/* State after n steps of the seed-chain (chain=1) or real (chain=0) LCG. */
+__device__ __forceinline__ uint64_t mcg_lcg_skip(uint64_t seed, uint64_t n, int chain)
+{
+  uint64_t a = chain ? MCG_RNGS_G : MCG_RNG_G, c = chain ? MCG_RNGS_C : MCG_RNG_C;
+  uint64_t A = 1, C = 0;
+  while (n) {
+    if (n & 1) {
+      A = A * a;
+      C = C * a + c;
+    }
+    c = c * a + c;
+    a = a * a;
+    n >>= 1;
+  }
+  return (A * seed + C) & MCG_MASK63;
+}
+
+__device__ __forceinline__ uint32_t mcg_hash_slot(uint32_t key, uint32_t mask)
+{
+  return (key * 0x9E3779B1u) & mask;
+}
+
+/* Bounded linear probe; returns true and the value if key is present. */
+__device__ __forceinline__ bool mcg_hash_find(const uint2 *tab, uint32_t mask, int probes,
+                                              uint32_t key, uint32_t &val)
+{
+  uint32_t slot = mcg_hash_slot(key, mask);
+  for (int p = 0; p < probes; ++p) {
+    uint2 e = __ldg(tab + slot);
+    if (e.x == key) {
+      val = e.y;
+      return true;
+    }
+    if (e.x == MCG_HASH_EMPTY)
+      return false;
+    slot = (slot + 1) & mask;
+  }
+  return false;
+}
+
+/* logf(x) bit-identical to the host C library, for x in (0, 1]; x == 0 gives
+ * -inf as the C library. */
+__device__ __forceinline__ float mcg_logf_strict(float x, const mcg_libm_tab *T,
+                                                 const mcg_libm_dev &L)
+{
+  if (x == 0.0f)
+    return -INFINITY;
+  float d;
+  float y = mcg_log_ff(x, &d, T);
+  if (d <= L.tau_log_max) {
+    uint32_t key = __float_as_uint(x);
+    if (d <= __ldg(L.tau_log + (key >> 19))) {
+      uint32_t v;
+      if (mcg_hash_find(L.hash_log, L.mask_log, L.probes_log, key, v))
+        y = __uint_as_float(v);
+    }
+  }
+  return y;
+}
+
+/* 1 - expf(t) with expf bit-identical to the host C library. */
+__device__ __forceinline__ float mcg_one_minus_expf_strict(float t, const mcg_libm_tab *T,
+                                                           const mcg_libm_dev &L)
+{
+  if (t < MCG_EXP_ONE_BOUND)
+    return 1.0f;
+  float d;
+  float y = mcg_exp_ff(t, &d, T);
+  if (d <= L.tau_exp_max) {
+    uint32_t key = __float_as_uint(t);
+    if (d <= __ldg(L.tau_exp + (key >> 19))) {
+      uint32_t v;
+      if (mcg_hash_find(L.hash_exp, L.mask_exp, L.probes_exp, key, v))
+        y = __uint_as_float(v);
+    }
+  }
+  return __fsub_rn(1.0f, y);
+}
+
+__device__ __forceinline__ float mcg_expf_strict(float t, const mcg_libm_tab *T,
+                                                 const mcg_libm_dev &L)
+{
+  float d;
+  float y = mcg_exp_ff(t, &d, T);
+  if (d <= L.tau_exp_max) {
+    uint32_t key = __float_as_uint(t);
+    if (d <= __ldg(L.tau_exp + (key >> 19))) {
+      uint32_t v;
+      if (mcg_hash_find(L.hash_exp, L.mask_exp, L.probes_exp, key, v))
+        y = __uint_as_float(v);
+    }
+  }
+  return y;
+}
+
+/* Fast build: 1 - e^t for t <= 0 to a few ulp without cancellation. */
+__device__ __forceinline__ float mcg_one_minus_exp_fast(float t)
+{
+  if (t > -0.25f) {
+    /* -expm1(t) = -t (1 + t/2 + t^2/6 + ... + t^6/5040) */
+    float p = fmaf(t, 1.0f / 5040.0f, 1.0f / 720.0f);
+    p = fmaf(t, p, 1.0f / 120.0f);
+    p = fmaf(t, p, 1.0f / 24.0f);
+    p = fmaf(t, p, 1.0f / 6.0f);
+    p = fmaf(t, p, 0.5f);
+    p = fmaf(t, p, 1.0f);
+    return -t * p;
+  }
+  return 1.0f - __expf(t);
+}
+
+/* Fixed-point deposit: llrint(dw * 2^S) (dw * 2^S is exact). */
+__device__ __forceinline__ long long mcg_to_fixed(float dw, float scale)
+{
+  return __float2ll_rn(__fmul_rn(dw, scale));
+}
+
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+#endif

@@ -1,0 +1,67 @@
+/*
+ * mcg_internal.h - context layout shared by the translation units of
+ * libmcgb300 (not part of the public ABI).
+ */
+#ifndef MCG_INTERNAL_H
+#define MCG_INTERNAL_H
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "exact_libm.h"
+#include "mcg_device.cuh"
+#include "mcgb300.h"
+
+struct mcg_ext; /* optional per-context state of the queue / batch / adjoint units */
+
+struct mcg_context {
+  int device = 0, mode = MCG_MODE_STRICT;
+  int sm_count = 0, smem_optin = 0, cc_major = 0, cc_minor = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float last_ms = 0.f;
+  int last_grid = 0, last_block = 0;
+  long long launches = 0;
+
+  /* chain of layers */
+  int n_layers = 0, n_cells = 0, cell_lo = 0;
+  float min_w = 0.f;
+  std::vector<int32_t> layer_start, layer_m;
+  std::vector<float> layer_dx, sigs, rates;
+  std::vector<float4> cells_strict, cells_fast;
+  float4 *d_cells_strict = nullptr, *d_cells_fast = nullptr;
+  unsigned long long *d_tally = nullptr;
+  int log2_scale = 40;
+  unsigned long long *d_counters = nullptr, *d_next = nullptr;
+
+  /* strict libm */
+  bool libm_loaded = false;
+  mcg_libm_dev libm = {};
+  mcg_libm_tab *libm_tab = nullptr;
+  uint32_t libm_n_log = 0, libm_n_exp = 0;
+
+  /* particle buffers of the host-pointer entry points */
+  mcg_particle *d_part = nullptr;
+  int32_t *d_res = nullptr;
+  int64_t *d_steps = nullptr, *d_scat = nullptr;
+  size_t scratch_cap = 0;
+
+  /* launch shape */
+  int block = 256, blocks_per_sm = 0, refill = 16;
+  uint32_t max_steps = 1u << 28; /* per-history step limit (MCG_ERR_LIMIT) */
+
+  std::vector<void *> owned; /* device allocations freed at destroy */
+  mcg_ext *ext = nullptr;
+};
+
+int mcg_fail(int code, const char *fmt, ...);
+int mcg_cuda_fail(cudaError_t e, const char *what);
+void mcg_cell_params(float sig, float rate, int gi, float dx, float4 &strict, float4 &fast);
+int mcg_track_launch(mcg_context *ctx, mcg_particle *d_particles, int64_t n, int32_t *d_results,
+                     int64_t *d_steps, int64_t *d_scatters, const mcg_source *src, int64_t first);
+int mcg_sync(mcg_context *ctx);
+void mcg_ext_destroy(mcg_context *ctx);
+
+#endif

@@ -1,0 +1,284 @@
+/*
+ * mcg_track.cuh - the history-based tracker.
+ *
+ * One lane carries one particle history at a time through the whole chain of
+ * layers (a sub-domain crossing is just the next cell's parameters, so the
+ * hand-over between sub-domains costs nothing).  The grid is persistent:
+ * every warp takes chunks of history indices from a global counter and
+ * refills finished lanes from its chunk every `refill_steps` steps, so warps
+ * stay full however uneven the history lengths are.  Deposits go to a
+ * shared-memory 64-bit fixed-point histogram (one copy per block, or one per
+ * warp when the chain is short) and are added to the global tally once per
+ * block at the end; the sums are exact, hence order-independent.
+ *
+ * The step follows Layer::particle_step (src/layer.cpp:123-190) and the loop
+ * Layer::simulate_particle (src/layer.cpp:192-218).
+ */
+#ifndef MCG_TRACK_CUH
+#define MCG_TRACK_CUH
+
+#include "mcg_device.cuh"
+#include "mcgb300.h"
+
+/* Per-cell step parameters.  strict: {sig_a, sig_i, edge_lo, edge_hi}
+ * fast: {sig_a, -ln2/sig_i (0 when sig_i <= EPS), edge_lo, edge_hi}
+ * edge_lo = (float)i * dx_layer, edge_hi = (float)(i+1) * dx_layer with the
+ * GLOBAL cell index i and the cell's own layer spacing (src/layer.cpp:146,150). */
+struct mcg_track_params {
+  const float4 *cells;
+  int32_t n_cells, cell_lo;
+  float min_w, q_scale;
+  mcg_particle *particles; /* NULL: source mode */
+  int32_t *results;
+  int64_t *steps, *scatters;
+  int64_t n, first;
+  mcg_source src;
+  unsigned long long *next;  /* work counter, starts at 0 */
+  unsigned long long *tally; /* [n_cells] fixed point */
+  unsigned long long *counters; /* mcg_counters fields */
+  mcg_libm_dev libm;
+  const mcg_libm_tab *libm_tab;
+  int32_t refill_steps;
+  int32_t tally_copies; /* 1 or warps per block */
+  int32_t chunk;        /* histories per warp grab (multiple of 32) */
+  uint32_t max_steps;
+};
+
+enum { MCG_CNT_HIST = 0, MCG_CNT_STEPS, MCG_CNT_SCAT, MCG_CNT_LEFT, MCG_CNT_RIGHT, MCG_CNT_KILL,
+       MCG_CNT_WLEFT, MCG_CNT_WRIGHT, MCG_CNT_WKILL, MCG_CNT_ERR, MCG_CNT_N };
+
+/* Particle k of a device-born source (see mcg_source in mcgb300.h). */
+__device__ __forceinline__ void mcg_source_particle(const mcg_source &S, int64_t k, uint64_t &seed,
+                                                    float &x, float &mu, float &wmc, int &idx)
+{
+  uint64_t s = S.seed_mode == 0 ? mcg_lcg_skip(S.base_seed, (uint64_t)k + 1, 1)
+                                : ((S.base_seed + (uint64_t)k) & MCG_MASK63);
+  float m = S.mu0;
+  if (S.isotropic == 1)
+    m = __fsub_rn(__fmul_rn(2.0f, mcg_rnd_real(s)), 1.0f);
+  else if (S.isotropic == 2)
+    m = mcg_rnd_real(s);
+  seed = s;
+  x = S.x0;
+  mu = m;
+  wmc = S.w0;
+  idx = S.cell0;
+}
+
+__device__ __forceinline__ void mcg_load_particle(const mcg_track_params &P, int64_t i,
+                                                  uint64_t &seed, float &x, float &mu, float &wmc,
+                                                  int &idx)
+{
+  if (P.particles) {
+    const unsigned long long *q = reinterpret_cast<const unsigned long long *>(P.particles + i);
+    unsigned long long a = q[0], b = q[1], c = q[2];
+    seed = a;
+    x = __uint_as_float((uint32_t)b);
+    mu = __uint_as_float((uint32_t)(b >> 32));
+    wmc = __uint_as_float((uint32_t)c);
+    idx = (int)(uint32_t)(c >> 32);
+  } else {
+    mcg_source_particle(P.src, P.first + i, seed, x, mu, wmc, idx);
+  }
+}
+
+template <bool STRICT>
+__global__ void __launch_bounds__(256) mcg_track_kernel(mcg_track_params P)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  mcg_libm_tab *T = reinterpret_cast<mcg_libm_tab *>(smem);
+  unsigned long long *s_cnt = reinterpret_cast<unsigned long long *>(smem + sizeof(mcg_libm_tab));
+  unsigned long long *s_tally = s_cnt + 16;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ncell = P.n_cells, lo = P.cell_lo, hi = P.cell_lo + P.n_cells;
+
+  if (STRICT) {
+    const float *src = reinterpret_cast<const float *>(P.libm_tab);
+    float *dst = reinterpret_cast<float *>(T);
+    for (int i = tid; i < (int)(sizeof(mcg_libm_tab) / 4); i += blockDim.x)
+      dst[i] = src[i];
+  }
+  if (tid < 16)
+    s_cnt[tid] = 0ull;
+  for (int i = tid; i < ncell * P.tally_copies; i += blockDim.x)
+    s_tally[i] = 0ull;
+  __syncthreads();
+  unsigned long long *my_tally = s_tally + (size_t)(warp % P.tally_copies) * ncell;
+
+  uint64_t seed = 0;
+  float x = 0.f, mu = 0.f, wmc = 0.f, inv_mu = 0.f;
+  int idx = 0;
+  int64_t hid = -1;
+  uint32_t nst = 0, nsc = 0;
+  bool active = false;
+  unsigned long long tot_steps = 0, tot_scat = 0;
+  long long pool_next = 0, pool_end = 0;
+  bool drained = false;
+  const float min_w = P.min_w, qs = P.q_scale;
+
+  for (;;) {
+    unsigned need = __ballot_sync(0xffffffffu, !active);
+    if (need) {
+      int cnt = __popc(need), rank = __popc(need & lanemask_lt());
+      long long avail = pool_end - pool_next, my = -1;
+      if (rank < avail)
+        my = pool_next + rank;
+      if (cnt > avail && !drained) {
+        unsigned long long base = 0;
+        if (lane == 0)
+          base = atomicAdd(P.next, (unsigned long long)P.chunk);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if ((long long)base >= P.n) {
+          drained = true;
+          pool_next = pool_end = 0;
+        } else {
+          long long end = min((long long)base + P.chunk, (long long)P.n);
+          long long r2 = rank - avail;
+          if (rank >= avail && r2 < end - (long long)base)
+            my = (long long)base + r2;
+          pool_next = min((long long)base + (cnt - avail), end);
+          pool_end = end;
+        }
+      } else {
+        pool_next += min((long long)cnt, avail);
+      }
+      if (!active && my >= 0) {
+        hid = my;
+        mcg_load_particle(P, hid, seed, x, mu, wmc, idx);
+        if (!STRICT)
+          inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
+        nst = nsc = 0;
+        active = true;
+      }
+    }
+    if (!__any_sync(0xffffffffu, active))
+      break;
+
+    for (int k = 0; k < P.refill_steps; ++k) {
+      if (!active)
+        break;
+      if (!((wmc >= min_w) && (idx < hi) && (idx >= lo)) || nst >= P.max_steps) {
+        /* history ends: classification of simulate_particle */
+        int r;
+        if (nst >= P.max_steps && (wmc >= min_w) && (idx < hi) && (idx >= lo))
+          r = 2;
+        else if (idx == lo - 1)
+          r = -1;
+        else if (idx == hi)
+          r = 1;
+        else if (wmc < min_w)
+          r = 0;
+        else
+          r = -1;
+        if (P.particles) {
+          unsigned long long *q = reinterpret_cast<unsigned long long *>(P.particles + hid);
+          q[0] = seed;
+          q[1] = (unsigned long long)__float_as_uint(x) |
+                 ((unsigned long long)__float_as_uint(mu) << 32);
+          q[2] = (unsigned long long)__float_as_uint(wmc) |
+                 ((unsigned long long)(uint32_t)idx << 32);
+        }
+        if (P.results)
+          P.results[hid] = r;
+        if (P.steps)
+          P.steps[hid] = nst;
+        if (P.scatters)
+          P.scatters[hid] = nsc;
+        atomicAdd(&s_cnt[MCG_CNT_HIST], 1ull);
+        long long wq = mcg_to_fixed(wmc, qs);
+        if (r == -1) {
+          atomicAdd(&s_cnt[MCG_CNT_LEFT], 1ull);
+          atomicAdd(&s_cnt[MCG_CNT_WLEFT], (unsigned long long)wq);
+        } else if (r == 1) {
+          atomicAdd(&s_cnt[MCG_CNT_RIGHT], 1ull);
+          atomicAdd(&s_cnt[MCG_CNT_WRIGHT], (unsigned long long)wq);
+        } else if (r == 0) {
+          atomicAdd(&s_cnt[MCG_CNT_KILL], 1ull);
+          atomicAdd(&s_cnt[MCG_CNT_WKILL], (unsigned long long)wq);
+        } else {
+          atomicOr(&s_cnt[MCG_CNT_ERR], 1ull);
+        }
+        tot_steps += nst;
+        tot_scat += nsc;
+        active = false;
+        break;
+      }
+      const float4 c = __ldg(P.cells + (idx - lo));
+      const float sig_a = c.x;
+      const float h = mcg_rnd_real(seed);
+      float di;
+      int inew;
+      float edge, de;
+      if (STRICT) {
+        /* di = sig_i > EPS ? -log(h) / sig_i : MAXREAL */
+        di = c.y > MCG_EPS ? __fdiv_rn(-mcg_logf_strict(h, T, P.libm), c.y) : MCG_MAXREAL;
+        const bool neg = mu < 0.0f;
+        inew = neg ? idx - 1 : idx + 1;
+        edge = neg ? c.z : c.w;
+        de = (mu < -MCG_EPS || MCG_EPS < mu) ? __fdiv_rn(__fsub_rn(edge, x), mu) : MCG_MAXREAL;
+        if (di < de) {
+          inew = idx;
+          x = __fadd_rn(x, __fmul_rn(di, mu));
+          mu = __fsub_rn(__fmul_rn(2.0f, mcg_rnd_real(seed)), 1.0f);
+          ++nsc;
+        } else {
+          di = de;
+          x = edge;
+        }
+        const float om = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, di), T, P.libm);
+        const float dw = __fmul_rn(om, wmc);
+        wmc = __fsub_rn(wmc, dw);
+        atomicAdd(&my_tally[idx - lo], (unsigned long long)mcg_to_fixed(dw, qs));
+      } else {
+        di = c.y != 0.0f ? __log2f(h) * c.y : MCG_MAXREAL;
+        const bool neg = mu < 0.0f;
+        inew = neg ? idx - 1 : idx + 1;
+        edge = neg ? c.z : c.w;
+        de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
+        if (di < de) {
+          inew = idx;
+          x = fmaf(di, mu, x);
+          mu = fmaf(2.0f, mcg_rnd_real(seed), -1.0f);
+          inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
+          ++nsc;
+        } else {
+          di = de;
+          x = edge;
+        }
+        const float dw = mcg_one_minus_exp_fast(-sig_a * di) * wmc;
+        wmc -= dw;
+        atomicAdd(&my_tally[idx - lo], (unsigned long long)mcg_to_fixed(dw, qs));
+      }
+      idx = inew;
+      ++nst;
+    }
+  }
+
+  /* per-thread counters -> block */
+  for (int o = 16; o > 0; o >>= 1) {
+    tot_steps += __shfl_down_sync(0xffffffffu, tot_steps, o);
+    tot_scat += __shfl_down_sync(0xffffffffu, tot_scat, o);
+  }
+  if (lane == 0) {
+    atomicAdd(&s_cnt[MCG_CNT_STEPS], tot_steps);
+    atomicAdd(&s_cnt[MCG_CNT_SCAT], tot_scat);
+  }
+  __syncthreads();
+  for (int i = tid; i < ncell; i += blockDim.x) {
+    unsigned long long s = 0;
+    for (int c = 0; c < P.tally_copies; ++c)
+      s += s_tally[(size_t)c * ncell + i];
+    if (s)
+      atomicAdd(&P.tally[i], s);
+  }
+  if (tid < MCG_CNT_N) {
+    if (tid == MCG_CNT_ERR) {
+      if (s_cnt[tid])
+        atomicOr(&P.counters[tid], s_cnt[tid]);
+    } else if (s_cnt[tid]) {
+      atomicAdd(&P.counters[tid], s_cnt[tid]);
+    }
+  }
+}
+
+#endif

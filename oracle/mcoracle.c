@@ -385,3 +385,12 @@ void orc_fp64_histories(const orc_layer *layers, int n_layers, const float *sigs
     leak[1] += lk1;
   }
 }
+
+/* The host C library's logf (fn 0) or expf (fn 1) over an array: the values
+ * the reference's particle_step obtains (src/layer.cpp:137, :175). */
+void orc_libm_array(int fn, const float *in, float *out, long long n)
+{
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < n; ++i)
+    out[i] = fn == 0 ? logf(in[i]) : expf(in[i]);
+}

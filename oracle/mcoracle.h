@@ -93,6 +93,9 @@ void orc_fp64_histories(const orc_layer *layers, int n_layers, const float *sigs
                         const float *rates, double min_w, const orc_particle *particles, int n,
                         double *tally, double *tally_sq_hist, double *leak, int nthreads);
 
+/* Host C library logf (fn 0) / expf (fn 1) over an array. */
+void orc_libm_array(int fn, const float *in, float *out, long long n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -80,6 +80,7 @@ def lib():
                                              C.POINTER(C.c_int64), C.c_int]
         L.orc_format_wa.restype = C.c_int
         L.orc_format_wa.argtypes = [C.POINTER(Layer), C.c_void_p, C.c_char_p, C.c_int]
+        L.orc_libm_array.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_longlong]
         L.orc_fp64_histories.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                          C.c_double, C.c_void_p, C.c_int, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_int]
@@ -213,3 +214,11 @@ def format_wa(L, tally_f32):
                             1 << 20)
     assert n >= 0
     return buf.value.decode()
+
+
+def libm_array(fn, x):
+    """Host C library logf (fn 0) or expf (fn 1) of a float32 array."""
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.empty_like(x)
+    lib().orc_libm_array(fn, _p(x), _p(out), len(x))
+    return out

@@ -180,4 +180,33 @@ int ref_decomposed(float x_min, float x_max, int nb_cells, int P, float min_w, c
   return cycles;
 }
 
+/* rnd_seed chain and one rnd_real step per seed, with the reference's own
+ * src/random.cpp (the CPU half of src/test_curandom.cu:23-37). */
+void ref_rng_chain(uint64_t start, int n, uint64_t *seeds_out, uint64_t *seeds_after, float *reals)
+{
+  seed_t s = start;
+  for (int i = 0; i < n; ++i) {
+    seeds_out[i] = rnd_seed(&s);
+    seed_t t = seeds_out[i];
+    reals[i] = rnd_real(&t);
+    seeds_after[i] = t;
+  }
+}
+
+/* src/test_async_serialization.cpp:6-31: FNV-1a over the bytes of the test
+ * particle, as the reference's struct lays them out. */
+int ref_particle_hash(void)
+{
+  Particle p{5127801, 0.172634512365276, 123.12342351, -1231.123486123, 2134512};
+  const char *data = (const char *)&p;
+  unsigned int hash = 0x811c9dc5, prime = 16777619;
+  for (int i = 0; i < (int)sizeof(p); ++i) {
+    hash = hash ^ data[i];
+    hash = hash * prime;
+  }
+  int res;
+  memcpy(&res, &hash, sizeof(res));
+  return res;
+}
+
 } /* extern "C" */

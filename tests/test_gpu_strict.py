@@ -1,0 +1,188 @@
+"""GPU parity of the strict tracker against the oracle and the reference's
+golden data: bit-exact per particle, exact fixed-point tallies.
+
+Mirrors src/test_layer.cpp (golden WA.out through the GPU Layer),
+src/test_culayer.cu (cusimulate vs CPU) and src/test_curandom.cu (RNG)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+f32 = np.float32
+SCALE = 40
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+@pytest.fixture(scope="module")
+def ctx(built, mcg):
+    c = mcg.Context(mode="strict")
+    yield c
+    c.close()
+
+
+def oracle_q(oracle, layers, sigs, rates, min_w, particles):
+    return oracle.simulate_histories(list(layers), sigs, rates, min_w, particles, 2.0 ** SCALE)
+
+
+@pytest.mark.parametrize("name", ["config0", "default1000", "sublayer"])
+def test_golden_traces_bit_exact(ctx, mcg, name):
+    g = load(f"traces_{name}.npz")
+    lt = g["layer"]
+    ctx.set_layers([int(lt[3])], [int(lt[4])], [f32(lt[2])], g["sigs"], g["rates"],
+                   float(g["min_w"]))
+    p = g["initial"].astype(mcg.PARTICLE_DTYPE).copy()
+    r = ctx.simulate(p)
+    assert p.tobytes() == g["final"].astype(mcg.PARTICLE_DTYPE).tobytes()
+    assert np.array_equal(r["results"], g["result"])
+    assert np.array_equal(r["steps"], g["steps"])
+    assert np.array_equal(r["scatters"], g["scatters"])
+
+
+def test_tally_fixed_point_exact(ctx, mcg, oracle):
+    """The int64 tally equals the oracle's sum of llrint(dw * 2^S)."""
+    g = load("traces_config0.npz")
+    lt = g["layer"]
+    L = oracle.layer_make(float(lt[0]), float(lt[1]), int(lt[3]), int(lt[4]))
+    ctx.set_layers([0], [int(lt[4])], [f32(lt[2])], g["sigs"], g["rates"], 1e-12)
+    p = g["initial"].astype(mcg.PARTICLE_DTYPE).copy()
+    ctx.simulate(p)
+    ref = oracle_q(oracle, [L], g["sigs"], g["rates"], 1e-12, g["initial"])
+    assert np.array_equal(ctx.tally_q(), ref["tally_q"])
+    c = ctx.counters()
+    assert c["histories"] == len(p) and c["steps"] == int(g["steps"].sum())
+    assert c["scatters"] == int(g["scatters"].sum())
+
+
+def test_decomposed_chain_bit_exact(ctx, mcg, oracle):
+    """64 sub-domains of a 10000-cell slab (per-layer dx, as decompose_domain)
+    in one context: per-particle and tally parity with the oracle's
+    layer-by-layer hand-over."""
+    nb, P, N = 10000, 64, 3000
+    st, m, dx, _, _ = mcg.layer_decomposition(0.0, 1.0, nb, P)
+    xc = (np.arange(nb) + 0.5) / nb
+    sa = (0.5 + 0.4 * np.sin(6 * np.pi * xc)).astype(np.float32)
+    ss = (2.0 + 1.5 * np.cos(4 * np.pi * xc)).astype(np.float32)
+    sigs = (sa + ss).astype(np.float32)
+    rates = (sa / sigs).astype(np.float32)
+    ctx.set_layers(st, m, dx, sigs, rates, 1e-12)
+    p = np.zeros(N, mcg.PARTICLE_DTYPE)
+    p["seed"] = oracle.rnd_seed_chain(5127801, N)
+    p["x"], p["mu"], p["wmc"], p["index"] = 0.0, 1.0, 1.0, 0
+    init = p.copy()
+    r = ctx.simulate(p)
+    layers = oracle.decompose(0.0, 1.0, nb, P)
+    ref = oracle_q(oracle, layers, sigs, rates, 1e-12, init)
+    assert p.tobytes() == ref["particles"].tobytes()
+    assert np.array_equal(r["steps"], ref["traces"]["steps"])
+    assert np.array_equal(r["results"], ref["traces"]["result"])
+    assert np.array_equal(ctx.tally_q(), ref["tally_q"])
+
+
+def test_source_mode_matches_host_particles(ctx, mcg, oracle):
+    """Device-born particles (seed chain jump-ahead) = host-built particles."""
+    nb = 100
+    g = load("traces_config0.npz")
+    ctx.set_layers([0], [nb], [f32(1.0 / nb)], g["sigs"], g["rates"], 1e-12)
+    ctx.simulate_source(0, 4000, seed_mode=0, base_seed=5127801, x0=0.0, mu0=1.0, w0=1.0)
+    q_src = ctx.tally_q()
+    c = ctx.counters()
+    assert c["steps"] == int(g["steps"].sum())
+    ctx.tally_reset()
+    p = g["initial"].astype(mcg.PARTICLE_DTYPE).copy()
+    ctx.simulate(p)
+    assert np.array_equal(ctx.tally_q(), q_src)
+
+
+def test_golden_wa_through_gpu_layer(mcg):
+    """src/test_layer.cpp through the GPU Layer: WA.out byte-identical."""
+    x_ini = f32(np.sqrt(f32(2.0)) / f32(2.0))
+    layer = mcg.decompose_domain(0.0, 1.0, x_ini, 1, 0, 100, 100, 0.0)
+    layer.simulate(-1)
+    with open(os.path.join(GOLDEN, "test_layer_WA.out")) as f:
+        assert layer.format_WA() == f.read()
+    assert layer.nb_disabled == 100
+
+
+def test_cusimulate_dropin(mcg, oracle):
+    """src/test_culayer.cu: 1000 cells, default physics, every particle's final
+    state written back, tallies within 1e-4 of the CPU (exact here)."""
+    n, m = 20000, 1000
+    L = oracle.decompose(0.0, 1.0, m, 1)[0]
+    sigs, rates = oracle.default_sigs(L)
+    x_ini = f32(np.sqrt(f32(2.0)) / f32(2.0))
+    ps = oracle.create_particles(L, float(x_ini), float(f32(1.0 / n)), n, 5127801)
+    cpu = oracle.layer_simulate(L, sigs, rates, 0.0, ps[::-1].copy(), n)
+    gp = ps.astype(mcg.PARTICLE_DTYPE).copy()
+    w = np.zeros(m, np.float32)
+    mcg.cusimulate(gp, sigs, rates, w, 0, m, L.dx)
+    assert gp.tobytes() == cpu["particles"][::-1].tobytes()
+    assert np.max(np.abs(w - cpu["tally_f32"])) < 1e-4
+
+
+def test_layer_api_simulate_batches(mcg, oracle):
+    """Layer.simulate(n) consumes from the back, classifies leavers in
+    processing order and accumulates weights_absorbed."""
+    layer = mcg.Layer(0.25, 0.5, 25, 25, 1e-12)
+    rng = np.random.default_rng(3)
+    p = np.zeros(5000, mcg.PARTICLE_DTYPE)
+    p["seed"] = rng.integers(0, 2**63, 5000, dtype=np.uint64)
+    p["x"] = f32(0.3)
+    p["mu"] = rng.uniform(-1, 1, 5000).astype(np.float32)
+    p["wmc"] = 1.0
+    p["index"] = 30
+    layer.particles = p.copy()
+    layer.simulate(3000)
+    assert len(layer.particles) == 2000
+    L = oracle.layer_make(0.25, 0.5, 25, 25)
+    ref = oracle.layer_simulate(L, layer.sigs, layer.absorption_rates, 1e-12, p.copy(), 3000)
+    res = ref["results"]
+    proc = ref["particles"][len(p) - 3000:][::-1]
+    assert layer.particles_left.tobytes() == proc[res == -1].tobytes()
+    assert layer.particles_right.tobytes() == proc[res == 1].tobytes()
+    assert layer.nb_disabled == int(np.count_nonzero(res == 0))
+    assert np.allclose(layer.weights_absorbed, ref["tally_f32"], rtol=1e-5, atol=1e-6)
+
+
+def test_rnd_real_device_kat(ctx, oracle):
+    """src/test_curandom.cu: device rnd_real == CPU, seeds and floats."""
+    import torch
+    g = load("rng_chain.npz")
+    seeds = torch.tensor(g["seeds"].view(np.int64), device="cuda")
+    reals = torch.empty(len(g["seeds"]), dtype=torch.float32, device="cuda")
+    ctx.rnd_real_device(seeds.data_ptr(), reals.data_ptr(), len(g["seeds"]))
+    assert np.array_equal(seeds.cpu().numpy().view(np.uint64), g["seeds_after"])
+    assert np.array_equal(reals.cpu().numpy().view(np.uint32), g["reals"].view(np.uint32))
+
+
+@pytest.mark.parametrize("fn", [0, 1])
+def test_strict_libm_exhaustive(ctx, oracle, fn):
+    """Every logf argument in (0, 1] and every expf argument in [-17.5, 89):
+    the GPU equals the host C library bit for bit."""
+    import torch
+    lo, hi = (1, 0x3F800000) if fn == 0 else (None, None)
+    if fn == 0:
+        ranges = [(1, 0x3F800000 + 1)]
+    else:
+        neg_hi = int(np.array([-17.5], np.float32).view(np.uint32)[0])
+        pos_hi = int(np.array([89.0], np.float32).view(np.uint32)[0])
+        ranges = [(0x80000000, neg_hi + 1), (0, pos_hi)]
+    chunk = 1 << 26
+    bad = 0
+    for a, b in ranges:
+        for s in range(a, b, chunk):
+            e = min(s + chunk, b)
+            u = np.arange(s, e, dtype=np.uint64).astype(np.uint32)
+            x = u.view(np.float32)
+            d_in = torch.from_numpy(x).cuda()
+            d_out = torch.empty_like(d_in)
+            ctx.libm_eval_device(fn, d_in.data_ptr(), d_out.data_ptr(), len(x))
+            gpu = d_out.cpu().numpy().view(np.uint32)
+            host = oracle.libm_array(fn, x).view(np.uint32)
+            bad += int(np.count_nonzero(gpu != host))
+    assert bad == 0
