@@ -149,6 +149,11 @@ int mcg_last_kernel_ms(mcg_context *ctx, float *ms);
  * steps between lane refills. */
 int mcg_set_launch(mcg_context *ctx, int32_t block, int32_t blocks_per_sm, int32_t refill_steps);
 
+/* Where the tracker accumulates deposits: 0 shared-memory 64-bit atomics,
+ * 1 shared-memory 32-bit halves with carry (default), 2 64-bit atomics on the
+ * global tally.  All three give the same exact sums. */
+int mcg_set_tally_mode(mcg_context *ctx, int32_t mode);
+
 /* Longest history, in steps, before the tracker stops it with result 2 and
  * the call returns MCG_ERR_LIMIT (default 2^28; the reference has none). */
 int mcg_set_step_limit(mcg_context *ctx, int64_t max_steps);

@@ -83,6 +83,7 @@ def load_library(path=None):
         "mcg_last_kernel_ms": (C.c_int, [vp, C.POINTER(C.c_float)]),
         "mcg_set_launch": (C.c_int, [vp, i32, i32, i32]),
         "mcg_set_step_limit": (C.c_int, [vp, i64]),
+        "mcg_set_tally_mode": (C.c_int, [vp, i32]),
         "mcg_cusimulate": (C.c_int, [C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, f32]),
         "mcg_rnd_real_device": (C.c_int, [vp, vp, vp, i64]),
         "mcg_libm_eval_device": (C.c_int, [vp, C.c_int, vp, vp, i64]),
@@ -204,6 +205,9 @@ class Context:
 
     def set_launch(self, block=0, blocks_per_sm=0, refill_steps=0):
         _check(self.lib.mcg_set_launch(self.h, block, blocks_per_sm, refill_steps))
+
+    def set_tally_mode(self, mode):
+        _check(self.lib.mcg_set_tally_mode(self.h, int(mode)))
 
     def simulate(self, particles, want_steps=True):
         """Histories of host particles (PARTICLE_DTYPE, updated in place).

@@ -49,7 +49,6 @@
 #define MCG_SUB(a, b) __fsub_rn((a), (b))
 #define MCG_MUL(a, b) __fmul_rn((a), (b))
 #define MCG_FMA(a, b, c) __fmaf_rn((a), (b), (c))
-#define MCG_RINT(a) rintf(a)
 MCG_HD uint32_t mcg_f2u(float f) { return __float_as_uint(f); }
 MCG_HD float mcg_u2f(uint32_t u) { return __uint_as_float(u); }
 #else
@@ -57,12 +56,18 @@ MCG_HD float mcg_u2f(uint32_t u) { return __uint_as_float(u); }
 #define MCG_SUB(a, b) ((a) - (b))
 #define MCG_MUL(a, b) ((a) * (b))
 #define MCG_FMA(a, b, c) fmaf((a), (b), (c))
-#define MCG_RINT(a) rintf(a)
 MCG_HD uint32_t mcg_f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
 MCG_HD float mcg_u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
 #endif
 
 #include "libm_tables.inc"
+
+/* Exact small-integer <-> float conversions through the 1.5 * 2^23 bias
+ * (|k| < 2^22), on the FP32/INT pipes rather than the conversion unit.
+ * mcg_rint_k returns RN-even(x) as an int, like rintf. */
+#define MCG_MAGIC 12582912.0f /* 1.5 * 2^23, bits 0x4b400000 */
+MCG_HD float mcg_int_to_float(int k) { return MCG_SUB(mcg_u2f(0x4b400000u + (uint32_t)k), MCG_MAGIC); }
+MCG_HD int mcg_rint_k(float x) { return (int)(mcg_f2u(MCG_ADD(x, MCG_MAGIC)) - 0x4b400000u); }
 
 /* Lookup tables of the evaluators.  Kernels stage one copy in shared memory
  * (lanes index it divergently) and pass its address. */
@@ -129,7 +134,7 @@ MCG_HD float mcg_log_ff(float x, float *delta, const mcg_libm_tab *T)
   float s_hi = MCG_ADD(r, hh);
   float s_lo = MCG_ADD(MCG_SUB(r, s_hi), hh);
   s_lo = MCG_ADD(s_lo, MCG_FMA(-0.5f, r2l, t3));
-  float kf = (float)k;
+  float kf = mcg_int_to_float(k);
   float kh = MCG_MUL(kf, MCG_LN2_HI);  /* exact */
   float km = MCG_MUL(kf, MCG_LN2_MID); /* exact */
   float kl = MCG_MUL(kf, MCG_LN2_LO);
@@ -154,8 +159,26 @@ MCG_HD float mcg_log_ff(float x, float *delta, const mcg_libm_tab *T)
 MCG_HD float mcg_exp_ff(float t, float *delta, const mcg_libm_tab *T)
 {
   if (!(t < 89.0f)) { *delta = 0.5f; return mcg_u2f(0x7f800000u); }
-  float kf = MCG_RINT(MCG_MUL(t, MCG_EXP_INV));
-  int k = (int)kf;
+  int k = mcg_rint_k(MCG_MUL(t, MCG_EXP_INV));
+  if (k == 0) {
+    /* |t| <= ln2/128: the general path below with every k-term zero and
+     * T = 1 (identical bits, fewer operations) */
+    float q2h = MCG_MUL(t, t);
+    float q2l = MCG_FMA(t, t, -q2h);
+    float h2h = MCG_MUL(0.5f, q2h);
+    float sh = MCG_ADD(t, h2h);
+    float sl = MCG_ADD(MCG_SUB(t, sh), h2h);
+    float Q = MCG_FMA(t, MCG_FMA(t, MCG_EXP_Q5, MCG_EXP_Q4), MCG_EXP_Q3);
+    sl = MCG_ADD(sl, MCG_ADD(MCG_MUL(0.5f, q2l), MCG_MUL(MCG_MUL(q2h, t), Q)));
+    float z = MCG_ADD(1.0f, sh);
+    float ze = MCG_ADD(MCG_SUB(1.0f, z), sh);
+    float lo = MCG_ADD(ze, sl);
+    float yh = MCG_ADD(z, lo);
+    float yl = MCG_ADD(MCG_SUB(z, yh), lo);
+    *delta = mcg_midpoint_delta(yh, yl);
+    return yh;
+  }
+  float kf = mcg_int_to_float(k);
   float p1 = MCG_MUL(kf, MCG_EXP_C1); /* exact */
   float r1 = MCG_SUB(t, p1);           /* exact */
   float p2 = MCG_MUL(kf, MCG_EXP_C2);
@@ -192,6 +215,31 @@ MCG_HD float mcg_exp_ff(float t, float *delta, const mcg_libm_tab *T)
   /* scale by 2^q, q in [-26, 128]; the product is exact unless it overflows */
   if (q > 127) { yh = MCG_MUL(yh, 2.0f); q -= 1; }
   return MCG_MUL(yh, mcg_u2f((uint32_t)(q + 127) << 23));
+}
+
+/* Cheap -log(x) for x in (0, 1] in plain float with the same argument
+ * reduction (about 2^-18 relative error).  The tracker only uses it to
+ * decide `di < d_edge` when the two are far apart; its largest relative
+ * deviation from the host C library's -logf over all of (0, 1) is measured
+ * exhaustively by the table generator and widens that margin. */
+MCG_HD float mcg_neglog_cheap(float x, const mcg_libm_tab *T)
+{
+  uint32_t u = mcg_f2u(x);
+  int kadj = 0;
+  if (u < 0x00800000u) {
+    x = MCG_MUL(x, 8388608.0f);
+    u = mcg_f2u(x);
+    kadj = -23;
+  }
+  int e = (int)(u >> 23) - 127;
+  uint32_t i = (u >> 16) & 127u;
+  uint32_t sel = i >> 6;
+  float m = mcg_u2f((u & 0x007fffffu) | (0x3f800000u - (sel << 23)));
+  float kf = mcg_int_to_float(e + (int)sel + kadj);
+  float r = MCG_FMA(m, T->log_invc[i], -1.0f);
+  float p = MCG_FMA(MCG_MUL(r, r), MCG_FMA(r, MCG_FMA(r, MCG_LOG_P4, MCG_LOG_P3), -0.5f), r);
+  float y = MCG_FMA(kf, MCG_LN2_HI, MCG_FMA(kf, MCG_LN2_MID, MCG_ADD(T->log_lhi[i], p)));
+  return -y;
 }
 
 /* Below this argument 1 - expf(t) rounds to exactly 1.0f whatever expf

@@ -144,6 +144,7 @@ static int load_libm(mcg_context *ctx)
   ctx->libm.hash_exp = dhe;
   ctx->libm_tab = dtab;
   ctx->libm_n_log = hdr.n_log;
+  ctx->cheap_log_relerr = hdr.cheap_log_relerr;
   ctx->libm_n_exp = hdr.n_exp;
   ctx->libm_loaded = true;
   return MCG_OK;
@@ -431,11 +432,19 @@ extern "C" int mcg_last_kernel_ms(mcg_context *ctx, float *ms)
 extern "C" int mcg_set_launch(mcg_context *ctx, int32_t block, int32_t blocks_per_sm,
                               int32_t refill_steps)
 {
-  if (!ctx || block < 0 || block > 256 || (block % 32) || blocks_per_sm < 0 || refill_steps < 0)
+  if (!ctx || block < 0 || block > 1024 || (block % 32) || blocks_per_sm < 0 || refill_steps < 0)
     return mcg_fail(MCG_ERR_ARG, "mcg_set_launch: bad arguments");
-  ctx->block = block ? block : 256;
+  ctx->block = block; /* 0: chosen per launch from the chain length */
   ctx->blocks_per_sm = blocks_per_sm;
-  ctx->refill = refill_steps ? refill_steps : 16;
+  ctx->refill = refill_steps ? refill_steps : 8;
+  return MCG_OK;
+}
+
+extern "C" int mcg_set_tally_mode(mcg_context *ctx, int32_t mode)
+{
+  if (!ctx || mode < 0 || mode > 2)
+    return mcg_fail(MCG_ERR_ARG, "mcg_set_tally_mode: mode must be 0, 1 or 2");
+  ctx->tally_mode = mode;
   return MCG_OK;
 }
 
@@ -467,7 +476,7 @@ int mcg_track_launch(mcg_context *ctx, mcg_particle *d_particles, int64_t n, int
   P.n_cells = ctx->n_cells;
   P.cell_lo = ctx->cell_lo;
   P.min_w = ctx->min_w;
-  P.q_scale = std::ldexp(1.0f, ctx->log2_scale);
+  P.q_log2 = ctx->log2_scale;
   P.particles = d_particles;
   P.results = d_results;
   P.steps = d_steps;
@@ -484,16 +493,30 @@ int mcg_track_launch(mcg_context *ctx, mcg_particle *d_particles, int64_t n, int
   P.refill_steps = ctx->refill;
   P.chunk = 64;
   P.max_steps = ctx->max_steps;
-  const int block = ctx->block, warps = block / 32;
+  P.cross_margin = 1.0f + ctx->cheap_log_relerr + 0x1p-21f;
+  /* default shape: short chains keep one tally copy per warp in 256-thread
+   * blocks; long chains share one copy per 1024-thread block */
+  int block = ctx->block;
+  if (block == 0)
+    block = ((size_t)ctx->n_cells * 8 * 8 <= 24 * 1024) ? 256 : 1024;
+  const int warps = block / 32;
   const size_t base = sizeof(mcg_libm_tab) + 16 * sizeof(unsigned long long);
+  int tmode = ctx->tally_mode;
   /* one tally copy per warp while it stays small, else one per block */
   int copies = ((size_t)ctx->n_cells * 8 * warps <= 24 * 1024) ? warps : 1;
-  size_t smem = base + (size_t)ctx->n_cells * 8 * copies;
-  if (smem > (size_t)ctx->smem_optin)
-    return mcg_fail(MCG_ERR_ARG, "chain of %d cells exceeds the shared-memory tally (max %d)",
-                    ctx->n_cells, (int)((ctx->smem_optin - base) / 8));
+  if (tmode != MCG_TALLY_GLOBAL && base + (size_t)ctx->n_cells * 8 > (size_t)ctx->smem_optin)
+    tmode = MCG_TALLY_GLOBAL; /* chain too long for a shared-memory copy */
+  size_t smem = base + (tmode == MCG_TALLY_GLOBAL ? 0 : (size_t)ctx->n_cells * 8 * copies);
   P.tally_copies = copies;
-  auto kern = strict ? mcg_track_kernel<true> : mcg_track_kernel<false>;
+  void (*kern)(mcg_track_params);
+  if (strict)
+    kern = tmode == MCG_TALLY_SMEM64 ? mcg_track_kernel<true, MCG_TALLY_SMEM64>
+         : tmode == MCG_TALLY_SMEM32 ? mcg_track_kernel<true, MCG_TALLY_SMEM32>
+                                     : mcg_track_kernel<true, MCG_TALLY_GLOBAL>;
+  else
+    kern = tmode == MCG_TALLY_SMEM64 ? mcg_track_kernel<false, MCG_TALLY_SMEM64>
+         : tmode == MCG_TALLY_SMEM32 ? mcg_track_kernel<false, MCG_TALLY_SMEM32>
+                                     : mcg_track_kernel<false, MCG_TALLY_GLOBAL>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess)
     return mcg_cuda_fail(e, "cudaFuncSetAttribute");

@@ -30,11 +30,30 @@ struct mcg_libm_dev {
   float tau_log_max, tau_exp_max;
 };
 
+/* RN((float)s) * 2^-63 for s < 2^63 with integer operations only: the
+ * hardware 64-bit integer-to-float conversion issues on the FP64 pipe, which
+ * GB300 provides at a small fraction of the FP32 rate.  Round to nearest,
+ * ties to even, as the reference's (float)seed (src/random.cpp:15). */
+__device__ __forceinline__ float mcg_u63_unit(uint64_t s)
+{
+  if (s == 0)
+    return 0.0f;
+  const uint32_t hi = (uint32_t)(s >> 32), lo = (uint32_t)s;
+  const int lz = hi ? __clz(hi) : 32 + __clz(lo);
+  const uint64_t m = s << lz; /* bit 63 set */
+  const uint32_t mh = (uint32_t)(m >> 32), ml = (uint32_t)m;
+  const uint32_t mant = mh >> 8, low8 = mh & 0xffu;
+  const uint32_t up = (low8 > 0x80u) | ((low8 == 0x80u) & ((ml != 0u) | (mant & 1u)));
+  /* value = s * 2^-63 has biased exponent 127 - lz; mant carries the
+   * implicit bit, and a rounding carry bumps the exponent */
+  return __uint_as_float(((uint32_t)(126 - lz) << 23) + mant + up);
+}
+
 /* rnd_real: s <- (G s + C) mod 2^63; h = RN((float)s) * 2^-63 */
 __device__ __forceinline__ float mcg_rnd_real(uint64_t &s)
 {
   s = (MCG_RNG_G * s + MCG_RNG_C) & MCG_MASK63;
-  return __fmul_rn(__ull2float_rn(s), 0x1p-63f);
+  return mcg_u63_unit(s);
 }
 
 __device__ __forceinline__ uint64_t mcg_rnd_seed(uint64_t &s)
@@ -154,10 +173,28 @@ __device__ __forceinline__ float mcg_one_minus_exp_fast(float t)
   return 1.0f - __expf(t);
 }
 
-/* Fixed-point deposit: llrint(dw * 2^S) (dw * 2^S is exact). */
-__device__ __forceinline__ long long mcg_to_fixed(float dw, float scale)
+/* Fixed-point deposit llrint(dw * 2^S), ties to even, with integer
+ * operations only (the hardware float-to-int64 conversion issues on the
+ * FP64 pipe).  Requires |dw| * 2^S < 2^63. */
+__device__ __forceinline__ long long mcg_to_fixed(float dw, int S)
 {
-  return __float2ll_rn(__fmul_rn(dw, scale));
+  const uint32_t u = __float_as_uint(dw);
+  const int e = (int)((u >> 23) & 0xffu);
+  const uint32_t mant = (u & 0x007fffffu) | 0x00800000u; /* dw = mant * 2^(e-150) */
+  const int sh = e - 150 + S;
+  uint64_t q;
+  if (e == 0) {
+    q = 0; /* zero or subnormal: |dw| 2^S < 2^-64 */
+  } else if (sh >= 0) {
+    q = (uint64_t)mant << sh;
+  } else if (sh >= -24) {
+    const int r = -sh;
+    const uint32_t qi = mant >> r, rem = mant & ((1u << r) - 1u), half = 1u << (r - 1);
+    q = qi + ((rem > half) | ((rem == half) & (qi & 1u)));
+  } else {
+    q = 0; /* below one half unit */
+  }
+  return (u >> 31) ? -(long long)q : (long long)q;
 }
 
 __device__ __forceinline__ unsigned lanemask_lt()

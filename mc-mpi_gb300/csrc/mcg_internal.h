@@ -41,6 +41,7 @@ struct mcg_context {
   mcg_libm_dev libm = {};
   mcg_libm_tab *libm_tab = nullptr;
   uint32_t libm_n_log = 0, libm_n_exp = 0;
+  float cheap_log_relerr = 1e-3f; /* replaced by the table's measured bound */
 
   /* particle buffers of the host-pointer entry points */
   mcg_particle *d_part = nullptr;
@@ -49,8 +50,9 @@ struct mcg_context {
   size_t scratch_cap = 0;
 
   /* launch shape */
-  int block = 256, blocks_per_sm = 0, refill = 16;
+  int block = 0, blocks_per_sm = 0, refill = 8;
   uint32_t max_steps = 1u << 28; /* per-history step limit (MCG_ERR_LIMIT) */
+  int tally_mode = 1;            /* MCG_TALLY_SMEM32 */
 
   std::vector<void *> owned; /* device allocations freed at destroy */
   mcg_ext *ext = nullptr;

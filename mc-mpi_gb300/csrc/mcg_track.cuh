@@ -27,7 +27,8 @@
 struct mcg_track_params {
   const float4 *cells;
   int32_t n_cells, cell_lo;
-  float min_w, q_scale;
+  float min_w;
+  int32_t q_log2;
   mcg_particle *particles; /* NULL: source mode */
   int32_t *results;
   int64_t *steps, *scatters;
@@ -42,7 +43,31 @@ struct mcg_track_params {
   int32_t tally_copies; /* 1 or warps per block */
   int32_t chunk;        /* histories per warp grab (multiple of 32) */
   uint32_t max_steps;
+  float cross_margin;   /* 1 + relative margin of the certain-crossing test */
 };
+
+/* Tally accumulation: shared-memory 64-bit atomics, shared-memory 32-bit
+ * halves with an explicit carry, or 64-bit atomics straight to the global
+ * tally (no shared memory, higher occupancy). */
+enum { MCG_TALLY_SMEM64 = 0, MCG_TALLY_SMEM32 = 1, MCG_TALLY_GLOBAL = 2 };
+
+template <int TALLY>
+__device__ __forceinline__ void mcg_tally_add(unsigned long long *t, long long q)
+{
+  if (TALLY == MCG_TALLY_SMEM32) {
+    /* exact 64-bit sum from 32-bit atomics: a carry out of the low word is
+     * detected by the adder that caused it and added to the high word */
+    const uint64_t v = (uint64_t)q;
+    const uint32_t lo = (uint32_t)v, hi = (uint32_t)(v >> 32);
+    unsigned *w = reinterpret_cast<unsigned *>(t);
+    const uint32_t old = atomicAdd(w, lo);
+    const uint32_t add_hi = hi + (((uint32_t)(old + lo) < old) ? 1u : 0u);
+    if (add_hi)
+      atomicAdd(w + 1, add_hi);
+  } else {
+    atomicAdd(t, (unsigned long long)q);
+  }
+}
 
 enum { MCG_CNT_HIST = 0, MCG_CNT_STEPS, MCG_CNT_SCAT, MCG_CNT_LEFT, MCG_CNT_RIGHT, MCG_CNT_KILL,
        MCG_CNT_WLEFT, MCG_CNT_WRIGHT, MCG_CNT_WKILL, MCG_CNT_ERR, MCG_CNT_N };
@@ -82,8 +107,8 @@ __device__ __forceinline__ void mcg_load_particle(const mcg_track_params &P, int
   }
 }
 
-template <bool STRICT>
-__global__ void __launch_bounds__(256) mcg_track_kernel(mcg_track_params P)
+template <bool STRICT, int TALLY>
+__global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   mcg_libm_tab *T = reinterpret_cast<mcg_libm_tab *>(smem);
@@ -100,10 +125,14 @@ __global__ void __launch_bounds__(256) mcg_track_kernel(mcg_track_params P)
   }
   if (tid < 16)
     s_cnt[tid] = 0ull;
-  for (int i = tid; i < ncell * P.tally_copies; i += blockDim.x)
-    s_tally[i] = 0ull;
+  if (TALLY != MCG_TALLY_GLOBAL)
+    for (int i = tid; i < ncell * P.tally_copies; i += blockDim.x)
+      s_tally[i] = 0ull;
   __syncthreads();
-  unsigned long long *my_tally = s_tally + (size_t)(warp % P.tally_copies) * ncell;
+  unsigned long long *my_tally = TALLY == MCG_TALLY_GLOBAL
+                                     ? P.tally
+                                     : s_tally + (size_t)(warp % P.tally_copies) * ncell;
+  const float cross_margin = P.cross_margin;
 
   uint64_t seed = 0;
   float x = 0.f, mu = 0.f, wmc = 0.f, inv_mu = 0.f;
@@ -114,7 +143,8 @@ __global__ void __launch_bounds__(256) mcg_track_kernel(mcg_track_params P)
   unsigned long long tot_steps = 0, tot_scat = 0;
   long long pool_next = 0, pool_end = 0;
   bool drained = false;
-  const float min_w = P.min_w, qs = P.q_scale;
+  const float min_w = P.min_w;
+  const int qs = P.q_log2;
 
   for (;;) {
     unsigned need = __ballot_sync(0xffffffffu, !active);
@@ -206,48 +236,65 @@ __global__ void __launch_bounds__(256) mcg_track_kernel(mcg_track_params P)
       const float4 c = __ldg(P.cells + (idx - lo));
       const float sig_a = c.x;
       const float h = mcg_rnd_real(seed);
-      float di;
-      int inew;
-      float edge, de;
+      const bool neg = mu < 0.0f;
+      int inew = neg ? idx - 1 : idx + 1;
+      const float edge = neg ? c.z : c.w;
+      float om;
       if (STRICT) {
-        /* di = sig_i > EPS ? -log(h) / sig_i : MAXREAL */
-        di = c.y > MCG_EPS ? __fdiv_rn(-mcg_logf_strict(h, T, P.libm), c.y) : MCG_MAXREAL;
-        const bool neg = mu < 0.0f;
-        inew = neg ? idx - 1 : idx + 1;
-        edge = neg ? c.z : c.w;
-        de = (mu < -MCG_EPS || MCG_EPS < mu) ? __fdiv_rn(__fsub_rn(edge, x), mu) : MCG_MAXREAL;
-        if (di < de) {
+        /* d_edge, and the crossing's absorption, do not depend on the flight
+         * sample: start them before the logarithm */
+        const float de =
+            (mu < -MCG_EPS || MCG_EPS < mu) ? __fdiv_rn(__fsub_rn(edge, x), mu) : MCG_MAXREAL;
+        const float om_cross = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, de), T, P.libm);
+        /* di = sig_i > EPS ? -log(h) / sig_i : MAXREAL; the exact value is
+         * only needed when the flight may end inside the cell: a cheap
+         * -log with a certified margin settles most crossings */
+        bool cross;
+        float di = MCG_MAXREAL;
+        if (c.y > MCG_EPS) {
+          const bool sure = h > 0.0f && c.y < 1e30f &&
+                            __fmul_rn(mcg_neglog_cheap(h, T), __frcp_rn(c.y)) >
+                                __fmul_rn(de, cross_margin);
+          if (sure) {
+            cross = true;
+          } else {
+            di = __fdiv_rn(-mcg_logf_strict(h, T, P.libm), c.y);
+            cross = !(di < de);
+          }
+        } else {
+          cross = !(di < de);
+        }
+        if (!cross) {
           inew = idx;
           x = __fadd_rn(x, __fmul_rn(di, mu));
           mu = __fsub_rn(__fmul_rn(2.0f, mcg_rnd_real(seed)), 1.0f);
+          om = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, di), T, P.libm);
           ++nsc;
         } else {
-          di = de;
           x = edge;
+          om = om_cross;
         }
-        const float om = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, di), T, P.libm);
         const float dw = __fmul_rn(om, wmc);
         wmc = __fsub_rn(wmc, dw);
-        atomicAdd(&my_tally[idx - lo], (unsigned long long)mcg_to_fixed(dw, qs));
+        mcg_tally_add<TALLY>(&my_tally[idx - lo], mcg_to_fixed(dw, qs));
       } else {
-        di = c.y != 0.0f ? __log2f(h) * c.y : MCG_MAXREAL;
-        const bool neg = mu < 0.0f;
-        inew = neg ? idx - 1 : idx + 1;
-        edge = neg ? c.z : c.w;
-        de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
+        const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
+        const float om_cross = mcg_one_minus_exp_fast(-sig_a * de);
+        const float di = c.y != 0.0f ? __log2f(h) * c.y : MCG_MAXREAL;
         if (di < de) {
           inew = idx;
           x = fmaf(di, mu, x);
           mu = fmaf(2.0f, mcg_rnd_real(seed), -1.0f);
           inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
+          om = mcg_one_minus_exp_fast(-sig_a * di);
           ++nsc;
         } else {
-          di = de;
           x = edge;
+          om = om_cross;
         }
-        const float dw = mcg_one_minus_exp_fast(-sig_a * di) * wmc;
+        const float dw = om * wmc;
         wmc -= dw;
-        atomicAdd(&my_tally[idx - lo], (unsigned long long)mcg_to_fixed(dw, qs));
+        mcg_tally_add<TALLY>(&my_tally[idx - lo], mcg_to_fixed(dw, qs));
       }
       idx = inew;
       ++nst;
@@ -264,13 +311,14 @@ __global__ void __launch_bounds__(256) mcg_track_kernel(mcg_track_params P)
     atomicAdd(&s_cnt[MCG_CNT_SCAT], tot_scat);
   }
   __syncthreads();
-  for (int i = tid; i < ncell; i += blockDim.x) {
-    unsigned long long s = 0;
-    for (int c = 0; c < P.tally_copies; ++c)
-      s += s_tally[(size_t)c * ncell + i];
-    if (s)
-      atomicAdd(&P.tally[i], s);
-  }
+  if (TALLY != MCG_TALLY_GLOBAL)
+    for (int i = tid; i < ncell; i += blockDim.x) {
+      unsigned long long s = 0;
+      for (int c = 0; c < P.tally_copies; ++c)
+        s += s_tally[(size_t)c * ncell + i];
+      if (s)
+        atomicAdd(&P.tally[i], s);
+    }
   if (tid < MCG_CNT_N) {
     if (tid == MCG_CNT_ERR) {
       if (s_cnt[tid])
