@@ -172,6 +172,31 @@ void cusimulate(int n, mcg_particle *particles, float const *const sigs,
 int mcg_cusimulate(int n, mcg_particle *particles, const float *sigs, const float *absorption_rates,
                    float *weights_absorbed, int min_index, int max_index, float dx);
 
+/* Fast tracker that allocates no device memory (no counterpart in the
+ * reference; this library's addition for callers that may not call
+ * cudaMalloc, such as host codes whose own allocator reserves the GPU's
+ * memory at start-up and forbids allocation afterwards).  Equivalent to a
+ * fast-mode context with mcg_set_layers + mcg_set_tally_scale(log2_scale) +
+ * mcg_simulate_device + mcg_tally_read: the caller passes the layers and
+ * cross sections (host arrays, as mcg_set_layers), the particles (device,
+ * updated in place), an optional device result array and the device output
+ * d_tally_q[total cells], which is overwritten with the fixed-point tally.
+ * Everything else lives in one statically sized device array inside the
+ * library, holding chains of at most MCG_NOALLOC_MAX_CELLS cells (larger
+ * chains are rejected with MCG_ERR_ARG).  The first call on a device looks
+ * up that array's device address (cudaGetSymbolAddress) with the current
+ * device; make that first call before any stream capture.  The array is
+ * shared by all calls on a device and keeps the last call's contents; each
+ * call clears what must start at zero.  Calls that overlap on the GPU race
+ * on it: serialise them.  Runs on the legacy default stream of the current
+ * device and returns when done. */
+#define MCG_NOALLOC_MAX_CELLS 16384
+int mcg_simulate_fast_noalloc(int n_layers, const int32_t *h_index_start, const int32_t *h_m,
+                              const float *h_dx, const float *h_sigs, const float *h_rates,
+                              float particle_min_weight, int32_t log2_scale,
+                              mcg_particle *d_particles, int64_t n, int32_t *d_results,
+                              int64_t *d_tally_q);
+
 /* One rnd_real step on n device seeds (src/curandom.cu:7-14). */
 int mcg_rnd_real_device(mcg_context *ctx, uint64_t *d_seeds, float *d_reals, int64_t n);
 
