@@ -172,6 +172,52 @@ void cusimulate(int n, mcg_particle *particles, float const *const sigs,
 int mcg_cusimulate(int n, mcg_particle *particles, const float *sigs, const float *absorption_rates,
                    float *weights_absorbed, int min_index, int max_index, float dx);
 
+/* ---- Batched slabs: thousands of independent slabs in one launch ----
+ * Slab s is a Layer(0, 1, 0, n_cells) (dx = 1/n_cells, both faces leak):
+ * a slab [0, L] maps onto it exactly by scaling its cross sections by L
+ * (sigs = (sigma_a + sigma_s) * L, rates = sigma_a / (sigma_a + sigma_s)).
+ * Its histories are particles 0 .. n_histories-1 of the source
+ * {seed_mode, isotropic, base_seed, x0 = 0, mu0, w0, cell 0} (mcg_source).
+ * Tallies are per slab and cell, concatenated in slab order. */
+typedef struct mcg_slab {
+  int32_t n_cells;
+  int32_t seed_mode;
+  int32_t isotropic;
+  int32_t reserved;
+  uint64_t base_seed;
+  int64_t n_histories;
+  float mu0, w0;
+} mcg_slab;
+/* h_sigs/h_rates: sum of n_cells entries, slab after slab.  Resets the
+ * batch tally. */
+int mcg_batch_set(mcg_context *ctx, int32_t n_slabs, const mcg_slab *h_slabs, const float *h_sigs,
+                  const float *h_rates, float particle_min_weight);
+/* Every history of every slab in one persistent launch, replayed from a
+ * CUDA graph (the graph is rebuilt when the launch shape changes).
+ * Accumulates into the batch tally; counters as mcg_counters_read. */
+int mcg_batch_run(mcg_context *ctx);
+/* The same work as one ordinary tracker launch per slab (the plain form),
+ * for comparison. */
+int mcg_batch_run_per_slab(mcg_context *ctx);
+int mcg_batch_tally_reset(mcg_context *ctx);
+int mcg_batch_tally_read(mcg_context *ctx, int64_t *h_q, double *h_f64);
+/* Launch shape of mcg_batch_run: threads per block (256, 512 or 1024),
+ * histories per work item (a block takes one item at a time), tally mode
+ * (as mcg_set_tally_mode). 0 keeps the current value. */
+int mcg_batch_set_launch(mcg_context *ctx, int32_t block, int64_t item_histories,
+                         int32_t tally_mode);
+/* Autotuner: times every candidate launch shape on a sample of each slab's
+ * histories (fraction in (0, 1]) and keeps the fastest.  Reports the choice
+ * and its sample time; the batch tally and counters are reset afterwards. */
+typedef struct mcg_batch_tuning {
+  int32_t block;
+  int32_t tally_mode;
+  int64_t item_histories;
+  float sample_ms;
+  int32_t candidates;
+} mcg_batch_tuning;
+int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_batch_tuning *out);
+
 /* Fast tracker that allocates no device memory (no counterpart in the
  * reference; this library's addition for callers that may not call
  * cudaMalloc, such as host codes whose own allocator reserves the GPU's

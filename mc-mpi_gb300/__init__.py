@@ -42,6 +42,20 @@ class Source(C.Structure):
                 ("x0", C.c_float), ("mu0", C.c_float), ("w0", C.c_float), ("cell0", C.c_int32)]
 
 
+class Slab(C.Structure):
+    _fields_ = [("n_cells", C.c_int32), ("seed_mode", C.c_int32), ("isotropic", C.c_int32),
+                ("reserved", C.c_int32), ("base_seed", C.c_uint64), ("n_histories", C.c_int64),
+                ("mu0", C.c_float), ("w0", C.c_float)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("block", C.c_int32), ("tally_mode", C.c_int32), ("item_histories", C.c_int64),
+                ("sample_ms", C.c_float), ("candidates", C.c_int32)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class Counters(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("histories", "steps", "scatters", "leaked_left",
                                          "leaked_right", "killed", "w_left_q", "w_right_q",
@@ -86,6 +100,13 @@ def load_library(path=None):
         "mcg_set_tally_mode": (C.c_int, [vp, i32]),
         "mcg_cusimulate": (C.c_int, [C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, f32]),
         "mcg_rnd_real_device": (C.c_int, [vp, vp, vp, i64]),
+        "mcg_batch_set": (C.c_int, [vp, i32, vp, vp, vp, f32]),
+        "mcg_batch_run": (C.c_int, [vp]),
+        "mcg_batch_run_per_slab": (C.c_int, [vp]),
+        "mcg_batch_tally_reset": (C.c_int, [vp]),
+        "mcg_batch_tally_read": (C.c_int, [vp, vp, vp]),
+        "mcg_batch_set_launch": (C.c_int, [vp, i32, i64, i32]),
+        "mcg_batch_autotune": (C.c_int, [vp, C.c_double, C.POINTER(Tuning)]),
         "mcg_libm_eval_device": (C.c_int, [vp, C.c_int, vp, vp, i64]),
     }
     for name, (res, args) in sig.items():
@@ -230,6 +251,48 @@ class Context:
                         w0=1.0, isotropic=0, cell0=0):
         src = Source(seed_mode, isotropic, base_seed, x0, mu0, w0, cell0)
         _check(self.lib.mcg_simulate_source(self.h, C.byref(src), int(first), int(n)))
+
+    # -- batched slabs --
+    def batch_set(self, slabs, sigs, rates, min_w):
+        """slabs: list of dicts(n_cells, n_histories, base_seed, seed_mode, isotropic, mu0, w0);
+        sigs/rates: concatenated per-cell arrays (slab order)."""
+        arr = (Slab * len(slabs))()
+        for i, d in enumerate(slabs):
+            arr[i] = Slab(int(d["n_cells"]), int(d.get("seed_mode", 0)), int(d.get("isotropic", 0)),
+                          0, int(d["base_seed"]), int(d["n_histories"]), float(d.get("mu0", 1.0)),
+                          float(d.get("w0", 1.0)))
+        sigs = np.ascontiguousarray(sigs, np.float32)
+        rates = np.ascontiguousarray(rates, np.float32)
+        _check(self.lib.mcg_batch_set(self.h, len(slabs), C.cast(arr, C.c_void_p), _ptr(sigs),
+                                      _ptr(rates), float(min_w)))
+        self.batch_cells = int(sum(int(d["n_cells"]) for d in slabs))
+
+    def batch_run(self):
+        _check(self.lib.mcg_batch_run(self.h))
+
+    def batch_run_per_slab(self):
+        _check(self.lib.mcg_batch_run_per_slab(self.h))
+
+    def batch_tally_reset(self):
+        _check(self.lib.mcg_batch_tally_reset(self.h))
+
+    def batch_tally_q(self):
+        out = np.zeros(self.batch_cells, np.int64)
+        _check(self.lib.mcg_batch_tally_read(self.h, _ptr(out), None))
+        return out
+
+    def batch_tally(self):
+        out = np.zeros(self.batch_cells, np.float64)
+        _check(self.lib.mcg_batch_tally_read(self.h, None, _ptr(out)))
+        return out
+
+    def batch_set_launch(self, block=0, item_histories=0, tally_mode=-1):
+        _check(self.lib.mcg_batch_set_launch(self.h, block, item_histories, tally_mode))
+
+    def batch_autotune(self, sample_fraction=0.02):
+        t = Tuning()
+        _check(self.lib.mcg_batch_autotune(self.h, float(sample_fraction), C.byref(t)))
+        return t.as_dict()
 
     def rnd_real_device(self, d_seeds, d_reals, n):
         _check(self.lib.mcg_rnd_real_device(self.h, C.c_void_p(d_seeds), C.c_void_p(d_reals), n))

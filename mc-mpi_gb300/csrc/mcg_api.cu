@@ -76,7 +76,7 @@ static int build_hash(const std::vector<uint32_t> &pairs, std::vector<uint2> &ta
   return MCG_OK;
 }
 
-static int load_libm(mcg_context *ctx)
+int mcg_load_libm(mcg_context *ctx)
 {
   if (ctx->libm_loaded)
     return MCG_OK;
@@ -198,7 +198,7 @@ extern "C" int mcg_create(int device, int mode, mcg_context **out)
     }
   }
   if (rc == MCG_OK && mode == MCG_MODE_STRICT)
-    rc = load_libm(ctx);
+    rc = mcg_load_libm(ctx);
   if (rc != MCG_OK) {
     std::string msg = g_last_error;
     mcg_destroy(ctx);
@@ -257,7 +257,7 @@ extern "C" int mcg_set_mode(mcg_context *ctx, int mode)
     return mcg_fail(MCG_ERR_ARG, "mcg_set_mode: bad arguments");
   int rc = ensure_device(ctx);
   if (rc == MCG_OK && mode == MCG_MODE_STRICT)
-    rc = load_libm(ctx);
+    rc = mcg_load_libm(ctx);
   if (rc == MCG_OK)
     ctx->mode = mode;
   return rc;
@@ -466,7 +466,7 @@ int mcg_track_launch(mcg_context *ctx, mcg_particle *d_particles, int64_t n, int
     return MCG_OK;
   const bool strict = ctx->mode == MCG_MODE_STRICT;
   if (strict && !ctx->libm_loaded) {
-    int rc = load_libm(ctx);
+    int rc = mcg_load_libm(ctx);
     if (rc != MCG_OK)
       return rc;
   }

@@ -14,7 +14,31 @@
 #include "mcg_device.cuh"
 #include "mcgb300.h"
 
-struct mcg_ext; /* optional per-context state of the queue / batch / adjoint units */
+/* Per-context state of the batched-slab unit (mcg_batch.cu). */
+struct mcg_batch_state {
+  int n_slabs = 0, total_cells = 0, max_cells = 0;
+  int64_t total_histories = 0;
+  std::vector<mcg_slab> slabs;
+  std::vector<int32_t> cell_off;
+  void *d_slabs = nullptr;  /* mcg_batch_slab_dev[] */
+  void *d_items = nullptr;  /* mcg_batch_item[] */
+  int n_items = 0, items_cap = 0;
+  float4 *d_cells_strict = nullptr, *d_cells_fast = nullptr;
+  unsigned long long *d_tally = nullptr;
+  unsigned long long *d_item_next = nullptr;
+  float min_w = 0.f;
+  /* launch shape, chosen by mcg_batch_set_launch or the autotuner */
+  int block = 512, tally_mode = 1;
+  int64_t item_histories = 16384;
+  /* CUDA graph of one run (memset of the item counter + the kernel) */
+  cudaGraphExec_t graph = nullptr;
+  bool graph_valid = false;
+  int items_built_for = -1; /* item size the list was built for */
+};
+
+struct mcg_ext {
+  mcg_batch_state batch;
+};
 
 struct mcg_context {
   int device = 0, mode = MCG_MODE_STRICT;
@@ -65,5 +89,6 @@ int mcg_track_launch(mcg_context *ctx, mcg_particle *d_particles, int64_t n, int
                      int64_t *d_steps, int64_t *d_scatters, const mcg_source *src, int64_t first);
 int mcg_sync(mcg_context *ctx);
 void mcg_ext_destroy(mcg_context *ctx);
+int mcg_load_libm(mcg_context *ctx);
 
 #endif

@@ -5,12 +5,6 @@
  */
 #include "mcg_internal.h"
 
-struct mcg_ext {};
-void mcg_ext_destroy(mcg_context *ctx)
-{
-  delete ctx->ext;
-  ctx->ext = nullptr;
-}
 
 __global__ void mcg_rnd_real_kernel(uint64_t *seeds, float *reals, int64_t n)
 {

@@ -107,6 +107,87 @@ __device__ __forceinline__ void mcg_load_particle(const mcg_track_params &P, int
   }
 }
 
+/* One Layer::particle_step (src/layer.cpp:123-190) on a lane's particle in
+ * cell c = {sig_a, sig_i or -ln2/sig_i, edge_lo, edge_hi}; deposits into
+ * *tally_cell.  STRICT: the reference's float operations and host-libm
+ * logf/expf; the crossing's absorption is computed before the logarithm and
+ * a certified cheap log settles most crossings.  FAST: hardware log2/exp2. */
+template <bool STRICT, int TALLY>
+__device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, float &wmc,
+                                         float &inv_mu, int &idx, uint32_t &nsc, const float4 c,
+                                         unsigned long long *tally_cell, int qs,
+                                         const mcg_libm_tab *T, const mcg_libm_dev &LM,
+                                         float cross_margin)
+{
+  const float sig_a = c.x;
+  const float h = mcg_rnd_real(seed);
+  const bool neg = mu < 0.0f;
+  int inew = neg ? idx - 1 : idx + 1;
+  const float edge = neg ? c.z : c.w;
+  float om;
+  if (STRICT) {
+    /* d_edge, and the crossing's absorption, do not depend on the flight
+     * sample: start them before the logarithm */
+    const float de =
+        (mu < -MCG_EPS || MCG_EPS < mu) ? __fdiv_rn(__fsub_rn(edge, x), mu) : MCG_MAXREAL;
+    const float om_cross = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, de), T, LM);
+    /* di = sig_i > EPS ? -log(h) / sig_i : MAXREAL; the exact value is
+     * only needed when the flight may end inside the cell: a cheap
+     * -log with a certified margin settles most crossings */
+    bool cross;
+    float di = MCG_MAXREAL;
+    if (c.y > MCG_EPS) {
+      const bool sure = h > 0.0f && c.y < 1e30f &&
+                        __fmul_rn(mcg_neglog_cheap(h, T), __frcp_rn(c.y)) >
+                            __fmul_rn(de, cross_margin);
+      if (sure) {
+        cross = true;
+      } else {
+        di = __fdiv_rn(-mcg_logf_strict(h, T, LM), c.y);
+        cross = !(di < de);
+      }
+    } else {
+      cross = !(di < de);
+    }
+    if (!cross) {
+      inew = idx;
+      x = __fadd_rn(x, __fmul_rn(di, mu));
+      mu = __fsub_rn(__fmul_rn(2.0f, mcg_rnd_real(seed)), 1.0f);
+      om = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, di), T, LM);
+      ++nsc;
+    } else {
+      x = edge;
+      om = om_cross;
+    }
+    const float dw = __fmul_rn(om, wmc);
+    wmc = __fsub_rn(wmc, dw);
+    mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dw, qs));
+  } else {
+    const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
+    const float om_cross = mcg_one_minus_exp_fast(-sig_a * de);
+    const float di = c.y != 0.0f ? __log2f(h) * c.y : MCG_MAXREAL;
+    if (di < de) {
+      inew = idx;
+      x = fmaf(di, mu, x);
+      mu = fmaf(2.0f, mcg_rnd_real(seed), -1.0f);
+      inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
+      om = mcg_one_minus_exp_fast(-sig_a * di);
+      ++nsc;
+    } else {
+      x = edge;
+      om = om_cross;
+    }
+    /* deposit the weight actually removed (exact by Sterbenz while the new
+     * weight is at least half the old), so the tally plus the surviving
+     * weights conserve the born weight to the fixed-point resolution */
+    const float wnew = __fsub_rn(wmc, __fmul_rn(om, wmc));
+    const float dep = __fsub_rn(wmc, wnew);
+    wmc = wnew;
+    mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dep, qs));
+  }
+  idx = inew;
+}
+
 template <bool STRICT, int TALLY>
 __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
 {
@@ -233,70 +314,8 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
         active = false;
         break;
       }
-      const float4 c = __ldg(P.cells + (idx - lo));
-      const float sig_a = c.x;
-      const float h = mcg_rnd_real(seed);
-      const bool neg = mu < 0.0f;
-      int inew = neg ? idx - 1 : idx + 1;
-      const float edge = neg ? c.z : c.w;
-      float om;
-      if (STRICT) {
-        /* d_edge, and the crossing's absorption, do not depend on the flight
-         * sample: start them before the logarithm */
-        const float de =
-            (mu < -MCG_EPS || MCG_EPS < mu) ? __fdiv_rn(__fsub_rn(edge, x), mu) : MCG_MAXREAL;
-        const float om_cross = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, de), T, P.libm);
-        /* di = sig_i > EPS ? -log(h) / sig_i : MAXREAL; the exact value is
-         * only needed when the flight may end inside the cell: a cheap
-         * -log with a certified margin settles most crossings */
-        bool cross;
-        float di = MCG_MAXREAL;
-        if (c.y > MCG_EPS) {
-          const bool sure = h > 0.0f && c.y < 1e30f &&
-                            __fmul_rn(mcg_neglog_cheap(h, T), __frcp_rn(c.y)) >
-                                __fmul_rn(de, cross_margin);
-          if (sure) {
-            cross = true;
-          } else {
-            di = __fdiv_rn(-mcg_logf_strict(h, T, P.libm), c.y);
-            cross = !(di < de);
-          }
-        } else {
-          cross = !(di < de);
-        }
-        if (!cross) {
-          inew = idx;
-          x = __fadd_rn(x, __fmul_rn(di, mu));
-          mu = __fsub_rn(__fmul_rn(2.0f, mcg_rnd_real(seed)), 1.0f);
-          om = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, di), T, P.libm);
-          ++nsc;
-        } else {
-          x = edge;
-          om = om_cross;
-        }
-        const float dw = __fmul_rn(om, wmc);
-        wmc = __fsub_rn(wmc, dw);
-        mcg_tally_add<TALLY>(&my_tally[idx - lo], mcg_to_fixed(dw, qs));
-      } else {
-        const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
-        const float om_cross = mcg_one_minus_exp_fast(-sig_a * de);
-        const float di = c.y != 0.0f ? __log2f(h) * c.y : MCG_MAXREAL;
-        if (di < de) {
-          inew = idx;
-          x = fmaf(di, mu, x);
-          mu = fmaf(2.0f, mcg_rnd_real(seed), -1.0f);
-          inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
-          om = mcg_one_minus_exp_fast(-sig_a * di);
-          ++nsc;
-        } else {
-          x = edge;
-          om = om_cross;
-        }
-        const float dw = om * wmc;
-        wmc -= dw;
-        mcg_tally_add<TALLY>(&my_tally[idx - lo], mcg_to_fixed(dw, qs));
-      }
-      idx = inew;
+      mcg_step<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + (idx - lo)),
+                              &my_tally[idx - lo], qs, T, P.libm, cross_margin);
       ++nst;
     }
   }
