@@ -79,6 +79,13 @@ int mcg_set_layers(mcg_context *ctx, int n_layers, const int32_t *h_index_start,
                    const int32_t *h_m, const float *h_dx, const float *h_sigs,
                    const float *h_rates, float particle_min_weight);
 
+/* As mcg_set_layers, with the step's two cross sections given per cell:
+ * h_sig_a (weight attenuation, sigs*rates in the reference) and h_sig_s
+ * (flight sampling, sigs*(1 - rates)); the parameters of the adjoint. */
+int mcg_set_layers_xs(mcg_context *ctx, int n_layers, const int32_t *h_index_start,
+                      const int32_t *h_m, const float *h_dx, const float *h_sig_a,
+                      const float *h_sig_s, float particle_min_weight);
+
 /* decompose_domain(x_min, x_max, ., n_layers, r, nb_cells, ., .) for every r,
  * then mcg_set_layers.  h_sigs/h_rates may be NULL: the constructor's
  * defaults sigs = expf(-x_mid), rates = 0.5 (src/layer.cpp:54-63). */
@@ -217,6 +224,25 @@ typedef struct mcg_batch_tuning {
   int32_t candidates;
 } mcg_batch_tuning;
 int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_batch_tuning *out);
+
+/* ---- Differentiation: forward tally + adjoint gradients of a tally loss ----
+ * Loss F = sum_c w_c a_c over the chain cells, a_c the weight absorbed in
+ * cell c per history.  Gradients with respect to sig_a[c] = sigs*rates and
+ * sig_s[c] = sigs*(1 - rates) of every chain cell: sig_a only attenuates the
+ * weight (pathwise derivative along the history), sig_s sets the flight
+ * distribution (likelihood-ratio score 1/sig_s - l for a collision, -l for a
+ * crossing, times the loss deposited from that step on).  Each history is
+ * run forward and then replayed from its source index; no path is stored.
+ * A slab [0, L] mapped onto [0, 1] by scaling sigma by L has
+ * dF/dsigma_physical = L * dF/dsig. */
+int mcg_adjoint_set_weights(mcg_context *ctx, const float *h_w);
+int mcg_adjoint_reset(mcg_context *ctx); /* also resets the tally */
+/* Histories first .. first+n-1 of the source; with_gradient 0 runs the
+ * forward pass only (tally + loss).  Accumulates. */
+int mcg_adjoint_run(mcg_context *ctx, const mcg_source *src, int64_t first, int64_t n,
+                    int32_t with_gradient);
+/* Means per history since the last reset; any pointer may be NULL. */
+int mcg_adjoint_read(mcg_context *ctx, double *h_loss, double *h_grad_sig_a, double *h_grad_sig_s);
 
 /* Fast tracker that allocates no device memory (no counterpart in the
  * reference; this library's addition for callers that may not call

@@ -86,6 +86,7 @@ def load_library(path=None):
         "mcg_set_mode": (C.c_int, [vp, C.c_int]),
         "mcg_set_layers": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp, f32]),
         "mcg_set_slab": (C.c_int, [vp, f32, f32, i32, i32, vp, vp, f32]),
+        "mcg_set_layers_xs": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp, f32]),
         "mcg_set_tally_scale": (C.c_int, [vp, i32]),
         "mcg_tally_reset": (C.c_int, [vp]),
         "mcg_tally_read": (C.c_int, [vp, vp, vp]),
@@ -100,6 +101,10 @@ def load_library(path=None):
         "mcg_set_tally_mode": (C.c_int, [vp, i32]),
         "mcg_cusimulate": (C.c_int, [C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, f32]),
         "mcg_rnd_real_device": (C.c_int, [vp, vp, vp, i64]),
+        "mcg_adjoint_set_weights": (C.c_int, [vp, vp]),
+        "mcg_adjoint_reset": (C.c_int, [vp]),
+        "mcg_adjoint_run": (C.c_int, [vp, C.POINTER(Source), i64, i64, i32]),
+        "mcg_adjoint_read": (C.c_int, [vp, vp, vp, vp]),
         "mcg_batch_set": (C.c_int, [vp, i32, vp, vp, vp, f32]),
         "mcg_batch_run": (C.c_int, [vp]),
         "mcg_batch_run_per_slab": (C.c_int, [vp]),
@@ -190,6 +195,16 @@ class Context:
                                        _ptr(sigs), _ptr(rates), float(min_w)))
         self.n_cells = int(m.sum())
 
+    def set_layers_xs(self, index_start, m, dx, sig_a, sig_s, min_w):
+        index_start = np.ascontiguousarray(index_start, np.int32)
+        m = np.ascontiguousarray(m, np.int32)
+        dx = np.ascontiguousarray(dx, np.float32)
+        sig_a = np.ascontiguousarray(sig_a, np.float32)
+        sig_s = np.ascontiguousarray(sig_s, np.float32)
+        _check(self.lib.mcg_set_layers_xs(self.h, len(m), _ptr(index_start), _ptr(m), _ptr(dx),
+                                          _ptr(sig_a), _ptr(sig_s), float(min_w)))
+        self.n_cells = int(m.sum())
+
     def set_slab(self, x_min, x_max, nb_cells, n_layers=1, sigs=None, rates=None, min_w=0.0):
         s = None if sigs is None else np.ascontiguousarray(sigs, np.float32)
         r = None if rates is None else np.ascontiguousarray(rates, np.float32)
@@ -251,6 +266,27 @@ class Context:
                         w0=1.0, isotropic=0, cell0=0):
         src = Source(seed_mode, isotropic, base_seed, x0, mu0, w0, cell0)
         _check(self.lib.mcg_simulate_source(self.h, C.byref(src), int(first), int(n)))
+
+    # -- adjoint --
+    def adjoint_set_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        _check(self.lib.mcg_adjoint_set_weights(self.h, _ptr(w)))
+
+    def adjoint_reset(self):
+        _check(self.lib.mcg_adjoint_reset(self.h))
+
+    def adjoint_run(self, first, n, with_gradient=True, seed_mode=0, base_seed=5127801, x0=0.0,
+                    mu0=1.0, w0=1.0, isotropic=0, cell0=0):
+        src = Source(seed_mode, isotropic, base_seed, x0, mu0, w0, cell0)
+        _check(self.lib.mcg_adjoint_run(self.h, C.byref(src), int(first), int(n),
+                                        1 if with_gradient else 0))
+
+    def adjoint_read(self):
+        loss = C.c_double()
+        ga = np.zeros(self.n_cells, np.float64)
+        gs = np.zeros(self.n_cells, np.float64)
+        _check(self.lib.mcg_adjoint_read(self.h, C.byref(loss), _ptr(ga), _ptr(gs)))
+        return loss.value, ga, gs
 
     # -- batched slabs --
     def batch_set(self, slabs, sigs, rates, min_w):

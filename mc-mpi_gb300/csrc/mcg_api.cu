@@ -322,6 +322,47 @@ extern "C" int mcg_set_layers(mcg_context *ctx, int n_layers, const int32_t *h_i
   return mcg_tally_reset(ctx);
 }
 
+/* Same as mcg_set_layers with the two cross sections of particle_step given
+ * per cell directly: sig_a (absorption) and sig_s (flight sampling). */
+extern "C" int mcg_set_layers_xs(mcg_context *ctx, int n_layers, const int32_t *h_index_start,
+                                 const int32_t *h_m, const float *h_dx, const float *h_sig_a,
+                                 const float *h_sig_s, float particle_min_weight)
+{
+  if (!ctx || n_layers <= 0 || !h_index_start || !h_m || !h_dx || !h_sig_a || !h_sig_s)
+    return mcg_fail(MCG_ERR_ARG, "mcg_set_layers_xs: bad arguments");
+  int total = 0;
+  for (int l = 0; l < n_layers; ++l) {
+    if (h_m[l] <= 0 || (l > 0 && h_index_start[l] != h_index_start[l - 1] + h_m[l - 1]))
+      return mcg_fail(MCG_ERR_ARG, "mcg_set_layers_xs: layer %d is empty or not contiguous", l);
+    total += h_m[l];
+  }
+  std::vector<float> sigs(total), rates(total);
+  for (int c = 0; c < total; ++c) {
+    sigs[c] = h_sig_a[c] + h_sig_s[c];
+    rates[c] = sigs[c] > 0.0f ? h_sig_a[c] / sigs[c] : 0.0f;
+  }
+  int rc = mcg_set_layers(ctx, n_layers, h_index_start, h_m, h_dx, sigs.data(), rates.data(),
+                          particle_min_weight);
+  if (rc != MCG_OK)
+    return rc;
+  /* replace the derived cross sections by the given ones */
+  int k = 0;
+  for (int l = 0; l < n_layers; ++l)
+    for (int j = 0; j < h_m[l]; ++j, ++k) {
+      float4 &cs = ctx->cells_strict[k], &cf = ctx->cells_fast[k];
+      cs.x = cf.x = h_sig_a[k];
+      cs.y = h_sig_s[k];
+      cf.y = h_sig_s[k] > 1e-4f ? (float)(-0.69314718055994530942 / (double)h_sig_s[k]) : 0.0f;
+    }
+  cudaError_t e;
+  if ((e = cudaMemcpy(ctx->d_cells_strict, ctx->cells_strict.data(), total * sizeof(float4),
+                      cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(ctx->d_cells_fast, ctx->cells_fast.data(), total * sizeof(float4),
+                      cudaMemcpyHostToDevice)) != cudaSuccess)
+    return mcg_cuda_fail(e, "mcg_set_layers_xs: upload");
+  return MCG_OK;
+}
+
 extern "C" int mcg_set_slab(mcg_context *ctx, float x_min, float x_max, int32_t nb_cells,
                             int32_t n_layers, const float *h_sigs, const float *h_rates,
                             float particle_min_weight)

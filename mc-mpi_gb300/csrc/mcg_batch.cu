@@ -229,11 +229,14 @@ static void batch_free(mcg_batch_state *B)
   *B = mcg_batch_state();
 }
 
+void mcg_adjoint_release(mcg_adj_state *A);
+
 void mcg_ext_destroy(mcg_context *ctx)
 {
   if (!ctx->ext)
     return;
   batch_free(&ctx->ext->batch);
+  mcg_adjoint_release(&ctx->ext->adj);
   delete ctx->ext;
   ctx->ext = nullptr;
 }

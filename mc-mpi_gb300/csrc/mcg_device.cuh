@@ -185,6 +185,8 @@ __device__ __forceinline__ long long mcg_to_fixed(float dw, int S)
   uint64_t q;
   if (e == 0) {
     q = 0; /* zero or subnormal: |dw| 2^S < 2^-64 */
+  } else if (sh > 38) {
+    q = 0x3fffffffffffffffull; /* beyond the tally's range (or inf): saturate */
   } else if (sh >= 0) {
     q = (uint64_t)mant << sh;
   } else if (sh >= -24) {

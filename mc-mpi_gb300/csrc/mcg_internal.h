@@ -36,8 +36,18 @@ struct mcg_batch_state {
   int items_built_for = -1; /* item size the list was built for */
 };
 
+/* Per-context state of the adjoint unit (mcg_adjoint.cu). */
+struct mcg_adj_state {
+  float2 *d_aux = nullptr;               /* {w_c, 1/sig_s} per chain cell */
+  unsigned long long *d_grad = nullptr;  /* grad_a[n], grad_s[n], loss */
+  int n = 0;
+  int64_t histories = 0;
+  int g_log2 = 36;
+};
+
 struct mcg_ext {
   mcg_batch_state batch;
+  mcg_adj_state adj;
 };
 
 struct mcg_context {

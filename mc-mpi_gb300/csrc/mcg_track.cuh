@@ -117,7 +117,8 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
                                          float &inv_mu, int &idx, uint32_t &nsc, const float4 c,
                                          unsigned long long *tally_cell, int qs,
                                          const mcg_libm_tab *T, const mcg_libm_dev &LM,
-                                         float cross_margin)
+                                         float cross_margin, float *l_out = nullptr,
+                                         bool *coll_out = nullptr, float *dep_out = nullptr)
 {
   const float sig_a = c.x;
   const float h = mcg_rnd_real(seed);
@@ -161,12 +162,23 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
     }
     const float dw = __fmul_rn(om, wmc);
     wmc = __fsub_rn(wmc, dw);
-    mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dw, qs));
+    if (tally_cell)
+      mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dw, qs));
+    if (l_out) {
+      *l_out = cross ? de : di;
+      *coll_out = !cross;
+      *dep_out = dw;
+    }
   } else {
     const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
     const float om_cross = mcg_one_minus_exp_fast(-sig_a * de);
     const float di = c.y != 0.0f ? __log2f(h) * c.y : MCG_MAXREAL;
-    if (di < de) {
+    const bool coll = di < de;
+    if (l_out) {
+      *l_out = coll ? di : de;
+      *coll_out = coll;
+    }
+    if (coll) {
       inew = idx;
       x = fmaf(di, mu, x);
       mu = fmaf(2.0f, mcg_rnd_real(seed), -1.0f);
@@ -183,7 +195,10 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
     const float wnew = __fsub_rn(wmc, __fmul_rn(om, wmc));
     const float dep = __fsub_rn(wmc, wnew);
     wmc = wnew;
-    mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dep, qs));
+    if (tally_cell)
+      mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dep, qs));
+    if (dep_out)
+      *dep_out = dep;
   }
   idx = inew;
 }

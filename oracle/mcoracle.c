@@ -394,3 +394,110 @@ void orc_libm_array(int fn, const float *in, float *out, long long n)
   for (long long i = 0; i < n; ++i)
     out[i] = fn == 0 ? logf(in[i]) : expf(in[i]);
 }
+
+/* FP64 adjoint estimator (statistical oracle of the GPU adjoint): per history
+ * a forward pass in double computing G = sum_k w_{c_k} dep_k, then a replay
+ * from the same seed accumulating
+ *   dG/dsig_a[c] += l_k (w_c W_k - (G - P_k))          (pathwise)
+ *   dG/dsig_s[c] += (1{collision}/sig_s - l_k) (G - P_{k-1})   (score)
+ * sig_a/sig_s/w indexed by global cell; sums over the n histories. */
+static int fp64_walk(const orc_layer *layers, int n_layers, const double *sa, const double *ss,
+                     const double *w, double min_w, const orc_particle *p0, double G,
+                     double *grad_a, double *grad_s, double *G_out)
+{
+  uint64_t s = p0->seed;
+  double x = p0->x, mu = p0->mu, W = p0->wmc, Gacc = 0.0, P = 0.0;
+  int idx = p0->index, k = 0;
+  while (k < n_layers - 1 && idx >= layers[k].index_start + layers[k].m)
+    ++k;
+  for (;;) {
+    const orc_layer *L = &layers[k];
+    if (!(W >= min_w))
+      break;
+    if (idx < L->index_start) {
+      if (L->left_border || k == 0)
+        break;
+      --k;
+      continue;
+    }
+    if (idx >= L->index_start + L->m) {
+      if (L->right_border || k == n_layers - 1)
+        break;
+      ++k;
+      continue;
+    }
+    s = (RNG_G * s + RNG_C) & MASK63;
+    double h = (double)s * 0x1p-63;
+    double di = ss[idx] > ORC_EPS ? -log(h) / ss[idx] : DBL_MAX;
+    double dx = (double)L->dx;
+    double edge = mu < 0 ? idx * dx : (idx + 1) * dx;
+    double de = (mu < -ORC_EPS || ORC_EPS < mu) ? (edge - x) / mu : DBL_MAX;
+    int nidx = mu < 0 ? idx - 1 : idx + 1;
+    int coll = di < de;
+    double l;
+    if (coll) {
+      nidx = idx;
+      l = di;
+      x += di * mu;
+      s = (RNG_G * s + RNG_C) & MASK63;
+      mu = 2.0 * ((double)s * 0x1p-63) - 1.0;
+    } else {
+      l = de;
+      x = edge;
+    }
+    double Wn = W * exp(-sa[idx] * l);
+    double g = w[idx] * (W - Wn);
+    if (grad_a) {
+      double vb = G - P;
+      P += g;
+      double va = G - P;
+      grad_a[idx] += l * (w[idx] * Wn - va);
+      grad_s[idx] += ((coll ? 1.0 / ss[idx] : 0.0) - l) * vb;
+    }
+    Gacc += g;
+    W = Wn;
+    idx = nidx;
+  }
+  if (G_out)
+    *G_out = Gacc;
+  return 0;
+}
+
+void orc_fp64_adjoint(const orc_layer *layers, int n_layers, const double *sig_a,
+                      const double *sig_s, const double *w, double min_w,
+                      const orc_particle *particles, int n, double *loss_sum, double *grad_a_sum,
+                      double *grad_s_sum, int nthreads)
+{
+  int total = layers[n_layers - 1].index_start + layers[n_layers - 1].m;
+#ifdef _OPENMP
+  if (nthreads > 0)
+    omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+  double loss = 0.0;
+#pragma omp parallel reduction(+ : loss)
+  {
+    double *ga = (double *)calloc((size_t)total, sizeof(double));
+    double *gs = (double *)calloc((size_t)total, sizeof(double));
+#pragma omp for schedule(dynamic, 64)
+    for (int i = 0; i < n; ++i) {
+      double G = 0.0;
+      fp64_walk(layers, n_layers, sig_a, sig_s, w, min_w, &particles[i], 0.0, NULL, NULL, &G);
+      if (grad_a_sum)
+        fp64_walk(layers, n_layers, sig_a, sig_s, w, min_w, &particles[i], G, ga, gs, NULL);
+      loss += G;
+    }
+#pragma omp critical
+    {
+      if (grad_a_sum)
+        for (int c = 0; c < total; ++c) {
+          grad_a_sum[c] += ga[c];
+          grad_s_sum[c] += gs[c];
+        }
+    }
+    free(ga);
+    free(gs);
+  }
+  *loss_sum += loss;
+}

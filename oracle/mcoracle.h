@@ -93,6 +93,13 @@ void orc_fp64_histories(const orc_layer *layers, int n_layers, const float *sigs
                         const float *rates, double min_w, const orc_particle *particles, int n,
                         double *tally, double *tally_sq_hist, double *leak, int nthreads);
 
+/* FP64 adjoint estimator: sums over n histories of the loss G = sum_k w dep_k
+ * and of its gradients with respect to sig_a and sig_s (global cells). */
+void orc_fp64_adjoint(const orc_layer *layers, int n_layers, const double *sig_a,
+                      const double *sig_s, const double *w, double min_w,
+                      const orc_particle *particles, int n, double *loss_sum, double *grad_a_sum,
+                      double *grad_s_sum, int nthreads);
+
 /* Host C library logf (fn 0) / expf (fn 1) over an array. */
 void orc_libm_array(int fn, const float *in, float *out, long long n);
 

@@ -80,6 +80,9 @@ def lib():
                                              C.POINTER(C.c_int64), C.c_int]
         L.orc_format_wa.restype = C.c_int
         L.orc_format_wa.argtypes = [C.POINTER(Layer), C.c_void_p, C.c_char_p, C.c_int]
+        L.orc_fp64_adjoint.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_double, C.c_void_p, C.c_int, C.POINTER(C.c_double),
+                                       C.c_void_p, C.c_void_p, C.c_int]
         L.orc_libm_array.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_longlong]
         L.orc_fp64_histories.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                          C.c_double, C.c_void_p, C.c_int, C.c_void_p,
@@ -222,3 +225,22 @@ def libm_array(fn, x):
     out = np.empty_like(x)
     lib().orc_libm_array(fn, _p(x), _p(out), len(x))
     return out
+
+
+def fp64_adjoint(layers, sig_a, sig_s, w, min_w, particles, nthreads=0, with_gradient=True):
+    """Sums over the histories of the loss and of dG/dsig_a, dG/dsig_s (FP64);
+    with_gradient=False runs the forward pass only (gradients returned as 0)."""
+    layers_arr = (Layer * len(layers))(*layers)
+    total = layers[-1].index_start + layers[-1].m
+    sa = np.ascontiguousarray(sig_a, np.float64)
+    ss = np.ascontiguousarray(sig_s, np.float64)
+    ww = np.ascontiguousarray(w, np.float64)
+    ga = np.zeros(total, np.float64)
+    gs = np.zeros(total, np.float64)
+    loss = C.c_double(0.0)
+    particles = np.ascontiguousarray(particles)
+    lib().orc_fp64_adjoint(C.cast(layers_arr, C.c_void_p), len(layers), _p(sa), _p(ss), _p(ww),
+                           float(min_w), _p(particles), len(particles), C.byref(loss),
+                           _p(ga) if with_gradient else None, _p(gs) if with_gradient else None,
+                           nthreads)
+    return loss.value, ga, gs
