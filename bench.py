@@ -11,6 +11,9 @@ The full problem is 1e8 histories; one bench step runs one batch of
 --batch consecutive histories of that source (default 1e7, so 10 steps
 cover the whole 1e8).  Synthetic data: the reference has no dataset.
 
+batched / adjoint : the metric's other two forms (batched slabs of
+        configuration 2, forward+adjoint of configuration 3), each timed with
+        CUDA events on its own launch.
 value : histories/s of the strict tracker with the batch's particles
         already resident in HBM (mcg_simulate_device), CUDA-event time of
         the kernel, L2 flushed (256 MB memset) between steps.
@@ -298,6 +301,9 @@ def run_gpu(args):
                            "peak_gops": sms * 128 * f_sm / 1e9, "frac": issue_frac},
         "clocks": clocks,
     }
+    if rank == 0 and not args.no_extra:
+        line["batched"] = bench_batched(mcg, args.mode, local)
+        line["adjoint"] = bench_adjoint(mcg, args.mode, local)
     if rank == 0 and ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:
@@ -306,6 +312,66 @@ def run_gpu(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def bench_batched(mcg, mode, device, scale=0.02, reps=2):
+    """Configuration 2 (4096 slabs, cells U{16..4096}, L ~ U[0.5, 5], per-cell
+    sigma_a ~ U[0.1, 5], sigma_s ~ U[0, 10], histories log-uniform in
+    [1e3, 1e6] scaled by `scale`): one persistent CUDA-graph launch against
+    one ordinary launch per slab, same histories, same tallies."""
+    from mc_mpi_gb300 import workloads
+    slabs, sigs, rates = workloads.config2(scale_histories=scale)
+    n = sum(d["n_histories"] for d in slabs)
+    with mcg.Context(mode=mode, device=device) as ctx:
+        ctx.set_tally_scale(32)
+        ctx.batch_set(slabs, sigs, rates, MIN_W)
+        ctx.batch_run()  # warm-up, builds the graph
+        ms = []
+        for _ in range(reps):
+            ctx.batch_tally_reset()
+            ctx.batch_run()
+            ms.append(ctx.last_kernel_ms())
+        q_batch = ctx.batch_tally_q()
+        steps = ctx.counters()["steps"]
+        ctx.batch_tally_reset()
+        ctx.batch_run_per_slab()
+        ms_plain = ctx.last_kernel_ms()
+        same = bool(np.array_equal(ctx.batch_tally_q(), q_batch))
+    t = min(ms) / 1e3
+    return {"value": n / t, "unit": "histories/s", "per_slab_value": n / (ms_plain / 1e3),
+            "speedup_vs_per_slab": (ms_plain / 1e3) / t, "identical_tallies": same,
+            "steps_per_s": steps / t, "histories": n, "launches": 1,
+            "workload": f"4096 slabs, cells U{{16..4096}}, L~U[0.5,5], sigma_a~U[0.1,5], "
+                        f"sigma_s~U[0,10], histories log-uniform [1e3,1e6] x {scale}"}
+
+
+def bench_adjoint(mcg, mode, device, n=10_000_000):
+    """Configuration 3 (1000 cells on [0, 2], sigma_a ~ U[0.2, 2], sigma_s ~
+    U[0.5, 5], loss weights ~ N(0, 1)): forward + adjoint of all 2,000 cross
+    sections against the forward pass alone, 1e7 histories."""
+    rng = np.random.default_rng(3)
+    M, L = 1000, np.float32(2.0)
+    sig_a = (rng.uniform(0.2, 2.0, M).astype(np.float32) * L).astype(np.float32)
+    sig_s = (rng.uniform(0.5, 5.0, M).astype(np.float32) * L).astype(np.float32)
+    w = rng.standard_normal(M).astype(np.float32)
+    with mcg.Context(mode=mode, device=device) as ctx:
+        ctx.set_layers_xs([0], [M], [np.float32(1.0 / M)], sig_a, sig_s, MIN_W)
+        ctx.adjoint_set_weights(w)
+        ctx.simulate_source(0, n // 10)  # warm-up
+        ctx.tally_reset()
+        ctx.simulate_source(0, n)
+        t_plain = ctx.last_kernel_ms() / 1e3
+        ctx.adjoint_reset()
+        ctx.adjoint_run(0, n, with_gradient=True)
+        t_adj = ctx.last_kernel_ms() / 1e3
+        ctx.adjoint_reset()
+        ctx.adjoint_run(0, n, with_gradient=False)
+        t_fwd = ctx.last_kernel_ms() / 1e3
+    return {"value": n / t_adj, "unit": "histories/s", "forward_value": n / t_plain,
+            "cost_vs_forward": t_adj / t_plain, "cost_vs_forward_with_loss": t_adj / t_fwd,
+            "parameters": 2 * M,
+            "workload": "1000 cells on [0,2], sigma_a~U[0.2,2], sigma_s~U[0.5,5], "
+                        "loss weights~N(0,1), 1e7 histories from x=0 mu=1"}
 
 
 def main():
@@ -317,6 +383,8 @@ def main():
     ap.add_argument("--mode", default="strict", choices=["strict", "fast"])
     ap.add_argument("--batch", type=int, default=10_000_000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the batched and adjoint measurements")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

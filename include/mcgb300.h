@@ -156,6 +156,14 @@ int mcg_last_kernel_ms(mcg_context *ctx, float *ms);
  * steps between lane refills. */
 int mcg_set_launch(mcg_context *ctx, int32_t block, int32_t blocks_per_sm, int32_t refill_steps);
 
+/* Algorithm of the single-chain entry points: MCG_ALGO_HISTORY (default,
+ * one lane carries a history to its end) or MCG_ALGO_EVENT (structure-of-
+ * arrays particle buffers; each pass advances every live particle by
+ * steps_per_pass events, 1 = classic event-based, and compacts the
+ * survivors with warp ballots).  Both give identical results. */
+enum mcg_algorithm { MCG_ALGO_HISTORY = 0, MCG_ALGO_EVENT = 1 };
+int mcg_set_algorithm(mcg_context *ctx, int32_t algorithm, int32_t steps_per_pass);
+
 /* Where the tracker accumulates deposits: 0 shared-memory 64-bit atomics,
  * 1 shared-memory 32-bit halves with carry (default), 2 64-bit atomics on the
  * global tally.  All three give the same exact sums. */
@@ -178,6 +186,21 @@ void cusimulate(int n, mcg_particle *particles, float const *const sigs,
 /* Same, returning a status instead of exiting. */
 int mcg_cusimulate(int n, mcg_particle *particles, const float *sigs, const float *absorption_rates,
                    float *weights_absorbed, int min_index, int max_index, float dx);
+
+/* ---- The workers' cycle with on-device hand-over queues ----
+ * Drop-in for WorkerSync/WorkerAsync/WorkerRma::spin (src/worker_sync.cpp,
+ * src/worker_async.cpp, src/worker_rma.cpp) when every sub-domain (layer of
+ * the context's chain) lives on this GPU: each cycle every sub-domain
+ * simulates up to per_cycle particles of its queue inside its own cells;
+ * leavers are appended to the neighbour's queue (at most queue_capacity
+ * waiting particles per sub-domain, else MCG_ERR_OVERFLOW, as the
+ * reference's bounded buffers); the n particles of the source are fed to the
+ * sub-domain holding src->cell0; the loop ends when all n histories are
+ * finished.  Tallies and counters as the other entry points; *h_cycles and
+ * *h_handoffs (may be NULL) report the cycles run and the particles handed
+ * over between sub-domains. */
+int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n, int32_t per_cycle,
+                   int64_t queue_capacity, int64_t *h_cycles, int64_t *h_handoffs);
 
 /* ---- Batched slabs: thousands of independent slabs in one launch ----
  * Slab s is a Layer(0, 1, 0, n_cells) (dx = 1/n_cells, both faces leak):

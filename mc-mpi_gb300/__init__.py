@@ -94,11 +94,13 @@ def load_library(path=None):
         "mcg_simulate_device": (C.c_int, [vp, vp, i64, vp, vp, vp]),
         "mcg_simulate_source": (C.c_int, [vp, C.POINTER(Source), i64, i64]),
         "mcg_create_particles": (C.c_int, [vp, C.POINTER(Source), i64, i64, vp]),
+        "mcg_worker_run": (C.c_int, [vp, C.POINTER(Source), i64, i32, i64, vp, vp]),
         "mcg_counters_read": (C.c_int, [vp, C.POINTER(Counters)]),
         "mcg_last_kernel_ms": (C.c_int, [vp, C.POINTER(C.c_float)]),
         "mcg_set_launch": (C.c_int, [vp, i32, i32, i32]),
         "mcg_set_step_limit": (C.c_int, [vp, i64]),
         "mcg_set_tally_mode": (C.c_int, [vp, i32]),
+        "mcg_set_algorithm": (C.c_int, [vp, i32, i32]),
         "mcg_cusimulate": (C.c_int, [C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, f32]),
         "mcg_rnd_real_device": (C.c_int, [vp, vp, vp, i64]),
         "mcg_adjoint_set_weights": (C.c_int, [vp, vp]),
@@ -242,6 +244,10 @@ class Context:
     def set_launch(self, block=0, blocks_per_sm=0, refill_steps=0):
         _check(self.lib.mcg_set_launch(self.h, block, blocks_per_sm, refill_steps))
 
+    def set_algorithm(self, algorithm="history", steps_per_pass=1):
+        _check(self.lib.mcg_set_algorithm(self.h, 0 if algorithm == "history" else 1,
+                                          int(steps_per_pass)))
+
     def set_tally_mode(self, mode):
         _check(self.lib.mcg_set_tally_mode(self.h, int(mode)))
 
@@ -329,6 +335,16 @@ class Context:
         t = Tuning()
         _check(self.lib.mcg_batch_autotune(self.h, float(sample_fraction), C.byref(t)))
         return t.as_dict()
+
+    def worker_run(self, n, per_cycle=65536, queue_capacity=1 << 20, seed_mode=0,
+                   base_seed=5127801, x0=0.0, mu0=1.0, w0=1.0, isotropic=0, cell0=0):
+        """The workers' cycle with on-device hand-over queues; returns
+        (cycles, handoffs)."""
+        src = Source(seed_mode, isotropic, base_seed, x0, mu0, w0, cell0)
+        cyc, hand = C.c_int64(), C.c_int64()
+        _check(self.lib.mcg_worker_run(self.h, C.byref(src), int(n), int(per_cycle),
+                                       int(queue_capacity), C.byref(cyc), C.byref(hand)))
+        return cyc.value, hand.value
 
     def rnd_real_device(self, d_seeds, d_reals, n):
         _check(self.lib.mcg_rnd_real_device(self.h, C.c_void_p(d_seeds), C.c_void_p(d_reals), n))

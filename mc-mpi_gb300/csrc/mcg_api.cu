@@ -241,6 +241,8 @@ extern "C" int mcg_destroy(mcg_context *ctx)
   mcg_ext_destroy(ctx);
   for (void *p : ctx->owned)
     cudaFree(p);
+  for (void *p : ctx->event_owned)
+    cudaFree(p);
   if (ctx->ev0)
     cudaEventDestroy(ctx->ev0);
   if (ctx->ev1)
@@ -535,6 +537,10 @@ int mcg_track_launch(mcg_context *ctx, mcg_particle *d_particles, int64_t n, int
   P.chunk = 64;
   P.max_steps = ctx->max_steps;
   P.cross_margin = 1.0f + ctx->cheap_log_relerr + 0x1p-21f;
+  if (ctx->algorithm == MCG_ALGO_EVENT) {
+    ctx->launches++;
+    return mcg_event_run(ctx, P);
+  }
   /* default shape: short chains keep one tally copy per warp in 256-thread
    * blocks; long chains share one copy per 1024-thread block */
   int block = ctx->block;

@@ -50,6 +50,13 @@ struct mcg_ext {
   mcg_adj_state adj;
 };
 
+/* Structure-of-arrays particle buffer of the event-based tracker. */
+struct mcg_soa {
+  unsigned long long *seed;
+  float *x, *mu, *wmc;
+  int32_t *idx, *hid, *nst, *nsc;
+};
+
 struct mcg_context {
   int device = 0, mode = MCG_MODE_STRICT;
   int sm_count = 0, smem_optin = 0, cc_major = 0, cc_minor = 0;
@@ -88,6 +95,13 @@ struct mcg_context {
   uint32_t max_steps = 1u << 28; /* per-history step limit (MCG_ERR_LIMIT) */
   int tally_mode = 1;            /* MCG_TALLY_SMEM32 */
 
+  /* algorithm: history-based (default) or event-based with K events per pass */
+  int algorithm = MCG_ALGO_HISTORY, event_steps = 1, event_passes = 0;
+  mcg_soa event_buf[2] = {};
+  size_t event_cap = 0;
+  std::vector<void *> event_owned;
+  unsigned *event_count = nullptr;
+
   std::vector<void *> owned; /* device allocations freed at destroy */
   mcg_ext *ext = nullptr;
 };
@@ -100,5 +114,7 @@ int mcg_track_launch(mcg_context *ctx, mcg_particle *d_particles, int64_t n, int
 int mcg_sync(mcg_context *ctx);
 void mcg_ext_destroy(mcg_context *ctx);
 int mcg_load_libm(mcg_context *ctx);
+struct mcg_track_params;
+int mcg_event_run(mcg_context *ctx, mcg_track_params &P);
 
 #endif

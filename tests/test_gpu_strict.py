@@ -186,3 +186,64 @@ def test_strict_libm_exhaustive(ctx, oracle, fn):
             host = oracle.libm_array(fn, x).view(np.uint32)
             bad += int(np.count_nonzero(gpu != host))
     assert bad == 0
+
+
+def _slab(mcg, nb, P):
+    from mc_mpi_gb300 import workloads
+    sigs, rates = workloads.config1(nb)
+    st, m, dx, _, _ = mcg.layer_decomposition(0.0, 1.0, nb, P)
+    return st, m, dx, sigs, rates
+
+
+@pytest.mark.parametrize("mode", ["strict", "fast"])
+@pytest.mark.parametrize("k", [1, 16])
+def test_event_mode_identical_to_history(mcg, oracle, mode, k):
+    """The event-based tracker (SoA buffers, compaction) gives the history
+    tracker's results particle by particle."""
+    st, m, dx, sigs, rates = _slab(mcg, 2000, 16)
+    p = np.zeros(3000, mcg.PARTICLE_DTYPE)
+    p["seed"] = oracle.rnd_seed_chain(99, 3000)
+    p["mu"], p["wmc"] = 1.0, 1.0
+    with mcg.Context(mode=mode) as ctx:
+        ctx.set_layers(st, m, dx, sigs, rates, 1e-12)
+        a = p.copy()
+        ra = ctx.simulate(a)
+        qa, ca = ctx.tally_q(), ctx.counters()
+        ctx.tally_reset()
+        ctx.set_algorithm("event", k)
+        b = p.copy()
+        rb = ctx.simulate(b)
+        assert a.tobytes() == b.tobytes()
+        for key in ("results", "steps", "scatters"):
+            assert np.array_equal(ra[key], rb[key])
+        assert np.array_equal(ctx.tally_q(), qa)
+        assert ctx.counters() == ca
+
+
+@pytest.mark.parametrize("per_cycle", [500, 65536])
+def test_worker_handover_queues_match_fused(mcg, per_cycle):
+    """The workers' cycle with per-sub-domain queues (64 sub-domains) gives
+    the fused tracker's tallies exactly."""
+    st, m, dx, sigs, rates = _slab(mcg, 10000, 64)
+    with mcg.Context(mode="strict") as ctx:
+        ctx.set_layers(st, m, dx, sigs, rates, 1e-12)
+        ctx.simulate_source(0, 4000)
+        fused = ctx.tally_q()
+        steps = ctx.counters()["steps"]
+        ctx.tally_reset()
+        cycles, hand = ctx.worker_run(4000, per_cycle=per_cycle, queue_capacity=1 << 16)
+        assert np.array_equal(ctx.tally_q(), fused)
+        assert ctx.counters()["steps"] == steps
+        assert cycles > 10 and hand > 4000
+
+
+def test_worker_matches_reference_workersync_tally(mcg):
+    """Against the reference's own Layer::simulate driven by the WorkerSync
+    cycle (golden fixture): float tallies agree to float accuracy."""
+    g = load("decomposed_1000x8.npz")
+    st, m, dx, _, _ = mcg.layer_decomposition(0.0, 1.0, 1000, int(g["n_layers"]))
+    with mcg.Context(mode="strict") as ctx:
+        ctx.set_layers(st, m, dx, g["sigs"], g["rates"], float(g["min_w"]))
+        ctx.worker_run(len(g["particles"]), per_cycle=500, queue_capacity=1 << 14)
+        t = ctx.tally()
+    assert np.allclose(t, g["tally"], rtol=2e-5, atol=1e-4)
