@@ -374,6 +374,89 @@ def bench_adjoint(mcg, mode, device, n=10_000_000):
                         "loss weights~N(0,1), 1e7 histories from x=0 mu=1"}
 
 
+def run_workload(args):
+    """Full-size runs of the metric's other forms, one JSON line each:
+    batch   configuration 2 (4096 slabs, ~5.9e8 histories): batched launch vs
+            one launch per slab, autotuned;
+    adjoint configuration 3 (1e7 histories, 2,000 parameters): forward +
+            adjoint vs forward;
+    fit     configuration 4 (64 slabs, 1e6 histories per slab and step, 200
+            Adam steps): final relative L2 error of sigma_a, histories/s."""
+    import importlib.util
+    import torch
+    torch.cuda.set_device(0)
+    spec = importlib.util.spec_from_file_location(
+        "mc_mpi_gb300", os.path.join(ROOT, "mc-mpi_gb300", "__init__.py"),
+        submodule_search_locations=[os.path.join(ROOT, "mc-mpi_gb300")])
+    mcg = importlib.util.module_from_spec(spec)
+    sys.modules["mc_mpi_gb300"] = mcg
+    spec.loader.exec_module(mcg)
+    from mc_mpi_gb300 import workloads
+    base = {"metric": METRIC, "unit": "histories/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic"}
+    if args.workload == "batch":
+        slabs, sigs, rates = workloads.config2(scale_histories=args.scale)
+        n = sum(d["n_histories"] for d in slabs)
+        with mcg.Context(mode=args.mode) as ctx, ClockSampler(0) as clk:
+            ctx.set_tally_scale(30)
+            ctx.batch_set(slabs, sigs, rates, MIN_W)
+            tune = ctx.batch_autotune(0.05)
+            ctx.batch_run()
+            ms = []
+            for _ in range(args.steps):
+                ctx.batch_tally_reset()
+                ctx.batch_run()
+                ms.append(ctx.last_kernel_ms())
+            c = ctx.counters()
+            q = ctx.batch_tally_q()
+            ctx.batch_tally_reset()
+            ctx.batch_run_per_slab()
+            ms_plain = ctx.last_kernel_ms()
+            same = bool(np.array_equal(q, ctx.batch_tally_q()))
+        t = statistics.median(ms) / 1e3
+        base.update(value=n / t, ms_per_step=t * 1e3, gpu_launches=1,
+                    config={"workload": "configuration 2: 4096 slabs, cells U{16..4096}, "
+                                        "L~U[0.5,5], sigma_a~U[0.1,5], sigma_s~U[0,10], histories "
+                                        f"log-uniform [1e3,1e6] x {args.scale}", "histories": n,
+                            "mode": args.mode, "autotuned": tune, "l2": "inputs born on device"},
+                    per_slab_value=n / (ms_plain / 1e3), speedup_vs_per_slab=ms_plain / 1e3 / t,
+                    identical_tallies=same, steps_per_s=c["steps"] / t,
+                    clocks=clk.summary())
+    elif args.workload == "adjoint":
+        base.update(bench_adjoint(mcg, args.mode, 0))
+        base["config"] = {"workload": base.pop("workload"), "mode": args.mode}
+    elif args.workload == "fit":
+        slabs, hidden, sig_s = workloads.config4(histories=int(1e6 * args.scale))
+        tslabs = [dict(d, n_histories=int(1e7 * args.scale), base_seed=d["base_seed"] + 1)
+                  for d in slabs]
+        sigs = (hidden + sig_s).astype(np.float32)
+        rates = (hidden / sigs).astype(np.float32)
+        n_steps = 200
+        with mcg.Context(mode="fast") as ctx, ClockSampler(0) as clk:
+            ctx.batch_set(tslabs, sigs, rates, MIN_W)
+            ctx.batch_run()
+            npc = np.concatenate([np.full(d["n_cells"], d["n_histories"]) for d in tslabs])
+            target = ctx.batch_tally() / npc
+            ctx.fit_set(slabs, np.ones_like(hidden), sig_s, target, max_steps=n_steps)
+            ctx.fit_run(n_steps, lr=1e-2)
+            ms = ctx.last_kernel_ms()
+            sig, loss = ctx.fit_read()
+        hist = n_steps * sum(d["n_histories"] for d in slabs)
+        err0 = float(np.linalg.norm(1.0 - hidden) / np.linalg.norm(hidden))
+        err = float(np.linalg.norm(sig - hidden) / np.linalg.norm(hidden))
+        base.update(value=hist / (ms / 1e3), ms_per_step=ms / n_steps, gpu_launches=3 * n_steps,
+                    config={"workload": "configuration 4: 64 slabs, cells U{64..1024}, hidden "
+                                        "sigma_a=1+0.8sin(2pi k x+phi), sigma_s=1.5, 200 Adam "
+                                        f"steps lr 1e-2, {int(1e6 * args.scale)} histories per "
+                                        "slab and step, targets from "
+                                        f"{int(1e7 * args.scale)} per slab", "mode": "fast"},
+                    rel_l2_error=err, rel_l2_error_start=err0,
+                    loss_first=float(loss[0]), loss_last=float(loss[-1]), clocks=clk.summary())
+    print(json.dumps(base))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -383,11 +466,16 @@ def main():
     ap.add_argument("--mode", default="strict", choices=["strict", "fast"])
     ap.add_argument("--batch", type=int, default=10_000_000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "adjoint", "fit"])
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="fraction of the configuration's histories (batch, fit)")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the batched and adjoint measurements")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "plain":
+        return run_workload(args)
     return run_gpu(args)
 
 

@@ -267,6 +267,24 @@ int mcg_adjoint_run(mcg_context *ctx, const mcg_source *src, int64_t first, int6
 /* Means per history since the last reset; any pointer may be NULL. */
 int mcg_adjoint_read(mcg_context *ctx, double *h_loss, double *h_grad_sig_a, double *h_grad_sig_s);
 
+/* ---- Batched inverse fit of absorption cross sections ----
+ * Slabs as mcg_batch_set (n_histories = histories per slab and step), with
+ * starting sig_a, fixed sig_s (per cell, slab order, the step's two cross
+ * sections) and measured tallies h_target (weight absorbed per history, per
+ * cell).  mcg_fit_run performs Adam steps on L = sum_c (a_c - t_c)^2: each
+ * step is one batched forward+adjoint launch over all slabs (fast
+ * arithmetic; loss weights 2 (a - t) from the previous step's tally),
+ * followed by the Adam update, all replayed from one CUDA graph, each step on
+ * fresh histories.  At most max_steps steps in total per mcg_fit_set. */
+int mcg_fit_set(mcg_context *ctx, int32_t n_slabs, const mcg_slab *h_slabs, const float *h_sig_a0,
+                const float *h_sig_s, const double *h_target, float particle_min_weight,
+                int32_t max_steps);
+int mcg_fit_run(mcg_context *ctx, int32_t n_steps, float lr, float beta1, float beta2, float eps,
+                float sig_min);
+/* sig_a of every cell, loss of every step so far (max_steps entries), steps done. */
+int mcg_fit_read(mcg_context *ctx, float *h_sig_a, double *h_loss_hist, int32_t *h_steps);
+int mcg_fit_release(mcg_context *ctx);
+
 /* Fast tracker that allocates no device memory (no counterpart in the
  * reference; this library's addition for callers that may not call
  * cudaMalloc, such as host codes whose own allocator reserves the GPU's

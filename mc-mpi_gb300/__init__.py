@@ -107,6 +107,10 @@ def load_library(path=None):
         "mcg_adjoint_reset": (C.c_int, [vp]),
         "mcg_adjoint_run": (C.c_int, [vp, C.POINTER(Source), i64, i64, i32]),
         "mcg_adjoint_read": (C.c_int, [vp, vp, vp, vp]),
+        "mcg_fit_set": (C.c_int, [vp, i32, vp, vp, vp, vp, f32, i32]),
+        "mcg_fit_run": (C.c_int, [vp, i32, f32, f32, f32, f32, f32]),
+        "mcg_fit_read": (C.c_int, [vp, vp, vp, vp]),
+        "mcg_fit_release": (C.c_int, [vp]),
         "mcg_batch_set": (C.c_int, [vp, i32, vp, vp, vp, f32]),
         "mcg_batch_run": (C.c_int, [vp]),
         "mcg_batch_run_per_slab": (C.c_int, [vp]),
@@ -293,6 +297,35 @@ class Context:
         gs = np.zeros(self.n_cells, np.float64)
         _check(self.lib.mcg_adjoint_read(self.h, C.byref(loss), _ptr(ga), _ptr(gs)))
         return loss.value, ga, gs
+
+    # -- batched inverse fit --
+    @staticmethod
+    def _slab_array(slabs):
+        arr = (Slab * len(slabs))()
+        for i, d in enumerate(slabs):
+            arr[i] = Slab(int(d["n_cells"]), int(d.get("seed_mode", 0)), int(d.get("isotropic", 0)),
+                          0, int(d["base_seed"]), int(d["n_histories"]), float(d.get("mu0", 1.0)),
+                          float(d.get("w0", 1.0)))
+        return arr
+
+    def fit_set(self, slabs, sig_a0, sig_s, target, min_w=1e-12, max_steps=1000):
+        arr = self._slab_array(slabs)
+        sig_a0 = np.ascontiguousarray(sig_a0, np.float32)
+        sig_s = np.ascontiguousarray(sig_s, np.float32)
+        target = np.ascontiguousarray(target, np.float64)
+        _check(self.lib.mcg_fit_set(self.h, len(slabs), C.cast(arr, C.c_void_p), _ptr(sig_a0),
+                                    _ptr(sig_s), _ptr(target), float(min_w), int(max_steps)))
+        self.fit_cells, self.fit_max_steps = len(sig_a0), int(max_steps)
+
+    def fit_run(self, n_steps, lr=1e-2, beta1=0.9, beta2=0.999, eps=1e-8, sig_min=1e-3):
+        _check(self.lib.mcg_fit_run(self.h, int(n_steps), lr, beta1, beta2, eps, sig_min))
+
+    def fit_read(self):
+        sig = np.zeros(self.fit_cells, np.float32)
+        loss = np.zeros(self.fit_max_steps, np.float64)
+        st = C.c_int32()
+        _check(self.lib.mcg_fit_read(self.h, _ptr(sig), _ptr(loss), C.byref(st)))
+        return sig, loss[:st.value]
 
     # -- batched slabs --
     def batch_set(self, slabs, sigs, rates, min_w):

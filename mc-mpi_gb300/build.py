@@ -25,7 +25,7 @@ GEN = os.path.join(OUT, "libm_tablegen")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["mcg_api.cu", "mcg_misc.cu", "mcg_noalloc.cu", "mcg_batch.cu",
-              "mcg_adjoint.cu", "mcg_event.cu", "mcg_worker.cu"]
+              "mcg_adjoint.cu", "mcg_event.cu", "mcg_worker.cu", "mcg_fit.cu"]
 HOST_SOURCES = []
 
 

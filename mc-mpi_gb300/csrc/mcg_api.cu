@@ -239,6 +239,7 @@ extern "C" int mcg_destroy(mcg_context *ctx)
   free_geometry(ctx);
   free_scratch(ctx);
   mcg_ext_destroy(ctx);
+  mcg_fit_release(ctx);
   for (void *p : ctx->owned)
     cudaFree(p);
   for (void *p : ctx->event_owned)

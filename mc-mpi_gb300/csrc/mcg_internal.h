@@ -114,6 +114,7 @@ int mcg_track_launch(mcg_context *ctx, mcg_particle *d_particles, int64_t n, int
 int mcg_sync(mcg_context *ctx);
 void mcg_ext_destroy(mcg_context *ctx);
 int mcg_load_libm(mcg_context *ctx);
+extern "C" int mcg_fit_release(mcg_context *ctx);
 struct mcg_track_params;
 int mcg_event_run(mcg_context *ctx, mcg_track_params &P);
 

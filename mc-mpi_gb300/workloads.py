@@ -51,3 +51,34 @@ def config2(n_slabs=4096, seed=2, cells=(16, 4096), hist=(1e3, 1e6), scale_histo
                           seed_mode=0, isotropic=0 if s % 2 == 0 else 2, mu0=1.0, w0=1.0,
                           length=L))
     return slabs, np.concatenate(sigs), np.concatenate(rates)
+
+
+def config3(m=1000, length=2.0, seed=3):
+    """Differentiation: m cells on [0, L], sigma_a ~ U[0.2, 2], sigma_s ~
+    U[0.5, 5], loss weights ~ N(0, 1).  Returns the step's cross sections on
+    the unit slab (sigma * L) and the weights."""
+    rng = np.random.default_rng(seed)
+    sa = rng.uniform(0.2, 2.0, m).astype(np.float32)
+    ss = rng.uniform(0.5, 5.0, m).astype(np.float32)
+    w = rng.standard_normal(m).astype(np.float32)
+    L = np.float32(length)
+    return (sa * L).astype(np.float32), (ss * L).astype(np.float32), w
+
+
+def config4(n_slabs=64, cells=(64, 1024), seed=4, histories=1_000_000):
+    """Inverse fit: n_slabs slabs on [0, 1], cells ~ U{64..1024}; hidden
+    sigma_a(x) = 1 + 0.8 sin(2 pi k x + phi), k ~ U{1..4}, phi ~ U[0, 2 pi);
+    sigma_s = 1.5; sources at x = 0, mu = 1.  Returns (slab dicts with
+    `histories` per step, hidden sigma_a, sigma_s)."""
+    rng = np.random.default_rng(seed)
+    slabs, hidden, sig_s = [], [], []
+    for s in range(n_slabs):
+        m = int(rng.integers(cells[0], cells[1] + 1))
+        k = int(rng.integers(1, 5))
+        phi = float(rng.uniform(0.0, 2.0 * np.pi))
+        xc = (np.arange(m, dtype=np.float64) + 0.5) / m
+        hidden.append((1.0 + 0.8 * np.sin(2.0 * np.pi * k * xc + phi)).astype(np.float32))
+        sig_s.append(np.full(m, 1.5, np.float32))
+        slabs.append(dict(n_cells=m, n_histories=histories, base_seed=BASE_SEED + 104729 * s,
+                          seed_mode=0, isotropic=0, mu0=1.0, w0=1.0))
+    return slabs, np.concatenate(hidden), np.concatenate(sig_s)
