@@ -26,7 +26,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["mcg_api.cu", "mcg_misc.cu", "mcg_noalloc.cu", "mcg_batch.cu",
               "mcg_adjoint.cu", "mcg_event.cu", "mcg_worker.cu", "mcg_fit.cu"]
-HOST_SOURCES = []
+HOST_SOURCES = ["layer.cpp", "random.cpp", "worker.cpp"]
 
 
 def _run(cmd, **kw):

@@ -49,11 +49,16 @@ __device__ __forceinline__ float mcg_u63_unit(uint64_t s)
   return __uint_as_float(((uint32_t)(126 - lz) << 23) + mant + up);
 }
 
-/* rnd_real: s <- (G s + C) mod 2^63; h = RN((float)s) * 2^-63 */
+/* rnd_real: s <- (G s + C) mod 2^63; h = RN((float)s) * 2^-63.
+ * MCG_HW_U2F selects the hardware conversion (FP64 pipe) instead. */
 __device__ __forceinline__ float mcg_rnd_real(uint64_t &s)
 {
   s = (MCG_RNG_G * s + MCG_RNG_C) & MCG_MASK63;
+#ifdef MCG_HW_U2F
+  return __fmul_rn(__ull2float_rn(s), 0x1p-63f);
+#else
   return mcg_u63_unit(s);
+#endif
 }
 
 __device__ __forceinline__ uint64_t mcg_rnd_seed(uint64_t &s)
@@ -178,6 +183,10 @@ __device__ __forceinline__ float mcg_one_minus_exp_fast(float t)
  * FP64 pipe).  Requires |dw| * 2^S < 2^63. */
 __device__ __forceinline__ long long mcg_to_fixed(float dw, int S)
 {
+#ifdef MCG_HW_F2I
+  /* hardware conversion (FP64 pipe); dw * 2^S is exact */
+  return __float2ll_rn(__fmul_rn(dw, __int_as_float((127 + S) << 23)));
+#endif
   const uint32_t u = __float_as_uint(dw);
   const int e = (int)((u >> 23) & 0xffu);
   const uint32_t mant = (u & 0x007fffffu) | 0x00800000u; /* dw = mant * 2^(e-150) */
