@@ -106,7 +106,9 @@ int mcg_simulate(mcg_context *ctx, mcg_particle *h_particles, int64_t n, int32_t
                  int64_t *h_steps, int64_t *h_scatters);
 
 /* The same on device-resident buffers (no copies); enqueued on the
- * context's stream and waited for. */
+ * context's stream and waited for.  That stream is non-blocking: buffers
+ * written on another stream must be complete before the call (every
+ * device-pointer entry point below has the same rule). */
 int mcg_simulate_device(mcg_context *ctx, mcg_particle *d_particles, int64_t n,
                         int32_t *d_results, int64_t *d_steps, int64_t *d_scatters);
 
@@ -314,7 +316,8 @@ int mcg_simulate_fast_noalloc(int n_layers, const int32_t *h_index_start, const 
 int mcg_rnd_real_device(mcg_context *ctx, uint64_t *d_seeds, float *d_reals, int64_t n);
 
 /* Strict-mode libm on the GPU for n arguments (testing aid): fn 0 logf on
- * [0, 1], fn 1 expf on [-17.5, 89); other arguments give NaN. */
+ * [0, 1], fn 1 expf on [-17.5, 89) (other arguments give NaN); fn 2 the
+ * hardware 2^x of the strict tracker's certain-crossing test. */
 int mcg_libm_eval_device(mcg_context *ctx, int fn, const float *d_in, float *d_out, int64_t n);
 
 #ifdef __cplusplus

@@ -134,6 +134,15 @@ def _check(rc):
         raise MCGError(rc, load_library().mcg_last_error().decode())
 
 
+def _device_inputs_ready():
+    """The library works on its own non-blocking stream: before a call that
+    reads device memory written through torch, wait for torch's stream."""
+    import sys
+    torch = sys.modules.get("torch")
+    if torch is not None and torch.cuda.is_initialized():
+        torch.cuda.current_stream().synchronize()
+
+
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
@@ -267,6 +276,7 @@ class Context:
         return dict(results=res, steps=steps, scatters=scat)
 
     def simulate_device_ptr(self, d_particles, n, d_results=None, d_steps=None, d_scatters=None):
+        _device_inputs_ready()
         _check(self.lib.mcg_simulate_device(self.h, C.c_void_p(d_particles), int(n),
                                             C.c_void_p(d_results) if d_results else None,
                                             C.c_void_p(d_steps) if d_steps else None,
@@ -380,9 +390,11 @@ class Context:
         return cyc.value, hand.value
 
     def rnd_real_device(self, d_seeds, d_reals, n):
+        _device_inputs_ready()
         _check(self.lib.mcg_rnd_real_device(self.h, C.c_void_p(d_seeds), C.c_void_p(d_reals), n))
 
     def libm_eval_device(self, fn, d_in, d_out, n):
+        _device_inputs_ready()
         _check(self.lib.mcg_libm_eval_device(self.h, fn, C.c_void_p(d_in), C.c_void_p(d_out), n))
 
 

@@ -175,7 +175,11 @@ MCG_HD float mcg_exp_ff(float t, float *delta, const mcg_libm_tab *T)
     float lo = MCG_ADD(ze, sl);
     float yh = MCG_ADD(z, lo);
     float yl = MCG_ADD(MCG_SUB(z, yh), lo);
-    *delta = mcg_midpoint_delta(yh, yl);
+    /* mcg_midpoint_delta for yh in [0.99, 1.01]: the spacing on yl's side is
+     * 2^-24 below 1 (and below 1.0 itself), 2^-23 from 1 up */
+    const uint32_t ub = mcg_f2u(yh);
+    const bool below = ub < 0x3f800000u || (ub == 0x3f800000u && yl < 0.0f);
+    *delta = MCG_SUB(0.5f, MCG_MUL(fabsf(yl), below ? 16777216.0f : 8388608.0f));
     return yh;
   }
   float kf = mcg_int_to_float(k);
@@ -215,31 +219,6 @@ MCG_HD float mcg_exp_ff(float t, float *delta, const mcg_libm_tab *T)
   /* scale by 2^q, q in [-26, 128]; the product is exact unless it overflows */
   if (q > 127) { yh = MCG_MUL(yh, 2.0f); q -= 1; }
   return MCG_MUL(yh, mcg_u2f((uint32_t)(q + 127) << 23));
-}
-
-/* Cheap -log(x) for x in (0, 1] in plain float with the same argument
- * reduction (about 2^-18 relative error).  The tracker only uses it to
- * decide `di < d_edge` when the two are far apart; its largest relative
- * deviation from the host C library's -logf over all of (0, 1) is measured
- * exhaustively by the table generator and widens that margin. */
-MCG_HD float mcg_neglog_cheap(float x, const mcg_libm_tab *T)
-{
-  uint32_t u = mcg_f2u(x);
-  int kadj = 0;
-  if (u < 0x00800000u) {
-    x = MCG_MUL(x, 8388608.0f);
-    u = mcg_f2u(x);
-    kadj = -23;
-  }
-  int e = (int)(u >> 23) - 127;
-  uint32_t i = (u >> 16) & 127u;
-  uint32_t sel = i >> 6;
-  float m = mcg_u2f((u & 0x007fffffu) | (0x3f800000u - (sel << 23)));
-  float kf = mcg_int_to_float(e + (int)sel + kadj);
-  float r = MCG_FMA(m, T->log_invc[i], -1.0f);
-  float p = MCG_FMA(MCG_MUL(r, r), MCG_FMA(r, MCG_FMA(r, MCG_LOG_P4, MCG_LOG_P3), -0.5f), r);
-  float y = MCG_FMA(kf, MCG_LN2_HI, MCG_FMA(kf, MCG_LN2_MID, MCG_ADD(T->log_lhi[i], p)));
-  return -y;
 }
 
 /* Below this argument 1 - expf(t) rounds to exactly 1.0f whatever expf

@@ -18,7 +18,7 @@
 #include <stdint.h>
 #include <string.h>
 
-#define MCG_LIBM_MAGIC "MCGLIBM2"
+#define MCG_LIBM_MAGIC "MCGLIBM3"
 #ifndef MCG_TAU_BUCKETS
 #define MCG_TAU_BUCKETS 8192
 #endif
@@ -28,7 +28,7 @@ typedef struct mcg_libm_file {
   char libc_version[56];
   uint64_t fingerprint;
   uint32_t n_log, n_exp;
-  float cheap_log_relerr; /* max |mcg_neglog_cheap - (-logf)| / -logf on (0, 1) */
+  float logf_relerr; /* max |logf(x) - ln x| / |ln x| over floats x in (0, 1) */
   uint32_t reserved;
   float tau_log[MCG_TAU_BUCKETS];
   float tau_exp[MCG_TAU_BUCKETS];

@@ -48,7 +48,6 @@ struct mcg_adj_params {
   const mcg_libm_tab *libm_tab;
   int32_t refill_steps, chunk, with_grad;
   uint32_t max_steps;
-  float cross_margin;
 };
 
 /* float-float accumulation s += v (TwoSum) */
@@ -83,7 +82,7 @@ __global__ void __launch_bounds__(1024) mcg_adjoint_kernel(mcg_adj_params P)
   for (int i = tid; i < 2 * ncell; i += blockDim.x)
     s_tally[i] = 0ull; /* the tally and both float gradient arrays */
   __syncthreads();
-  const float min_w = P.min_w, cross_margin = P.cross_margin;
+  const float min_w = P.min_w;
   const int qs = P.q_log2, gs = P.g_log2;
 
   uint64_t seed = 0;
@@ -169,8 +168,8 @@ __global__ void __launch_bounds__(1024) mcg_adjoint_kernel(mcg_adj_params P)
       float l, dep;
       bool coll;
       mcg_step<STRICT, MCG_TALLY_SMEM32>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + c),
-                                         phase == 0 ? &s_tally[c] : nullptr, qs, T, P.libm,
-                                         cross_margin, &l, &coll, &dep);
+                                         phase == 0 ? &s_tally[c] : nullptr, qs, T, P.libm, &l,
+                                         &coll, &dep);
       const float g = __fmul_rn(ax.x, dep);
       if (phase == 0) {
         ff_add(G_hi, G_lo, g);
@@ -320,7 +319,6 @@ extern "C" int mcg_adjoint_run(mcg_context *ctx, const mcg_source *src, int64_t 
   P.chunk = 64;
   P.with_grad = with_gradient ? 1 : 0;
   P.max_steps = ctx->max_steps;
-  P.cross_margin = 1.0f + ctx->cheap_log_relerr + 0x1p-21f;
   const int block = ctx->block ? ctx->block : 512;
   const size_t smem = sizeof(mcg_libm_tab) + 16 * 8 + 2 * (size_t)ctx->n_cells * 8;
   if (smem > (size_t)ctx->smem_optin)

@@ -103,6 +103,11 @@ int mcg_load_libm(mcg_context *ctx)
     return mcg_fail(MCG_ERR_TABLES,
                     "libm exception table %s was made against another C library (%s); rebuild",
                     path.c_str(), hdr.libc_version);
+  if (!(hdr.logf_relerr <= MCG_LOGF_RELERR_MAX))
+    return mcg_fail(MCG_ERR_TABLES,
+                    "host logf relative error %.3e exceeds the %.3e the strict tracker's "
+                    "certain-crossing test assumes",
+                    (double)hdr.logf_relerr, (double)MCG_LOGF_RELERR_MAX);
   std::vector<uint2> hl, he;
   int rc;
   if ((rc = build_hash(lp, hl, ctx->libm.mask_log, ctx->libm.probes_log)) != MCG_OK)
@@ -144,7 +149,6 @@ int mcg_load_libm(mcg_context *ctx)
   ctx->libm.hash_exp = dhe;
   ctx->libm_tab = dtab;
   ctx->libm_n_log = hdr.n_log;
-  ctx->cheap_log_relerr = hdr.cheap_log_relerr;
   ctx->libm_n_exp = hdr.n_exp;
   ctx->libm_loaded = true;
   return MCG_OK;
@@ -238,8 +242,8 @@ extern "C" int mcg_destroy(mcg_context *ctx)
     cudaStreamSynchronize(ctx->stream);
   free_geometry(ctx);
   free_scratch(ctx);
-  mcg_ext_destroy(ctx);
   mcg_fit_release(ctx);
+  mcg_ext_destroy(ctx);
   for (void *p : ctx->owned)
     cudaFree(p);
   for (void *p : ctx->event_owned)
@@ -537,7 +541,6 @@ int mcg_track_launch(mcg_context *ctx, mcg_particle *d_particles, int64_t n, int
   P.refill_steps = ctx->refill;
   P.chunk = 64;
   P.max_steps = ctx->max_steps;
-  P.cross_margin = 1.0f + ctx->cheap_log_relerr + 0x1p-21f;
   if (ctx->algorithm == MCG_ALGO_EVENT) {
     ctx->launches++;
     return mcg_event_run(ctx, P);

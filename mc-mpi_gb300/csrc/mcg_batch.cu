@@ -48,7 +48,6 @@ struct mcg_batch_params {
   int32_t q_log2;
   int32_t refill_steps;
   uint32_t max_steps;
-  float cross_margin;
 };
 
 template <bool STRICT, int TALLY>
@@ -68,7 +67,7 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
   }
   if (tid < 16)
     s_cnt[tid] = 0ull;
-  const float min_w = P.min_w, cross_margin = P.cross_margin;
+  const float min_w = P.min_w;
   const int qs = P.q_log2;
   int cur = -1, m = 0;
   const float4 *cells = nullptr;
@@ -184,7 +183,7 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
           break;
         }
         mcg_step<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(cells + idx),
-                                &tally[idx], qs, T, P.libm, cross_margin);
+                                &tally[idx], qs, T, P.libm);
         ++nst;
       }
     }
@@ -384,7 +383,6 @@ static int batch_configure(mcg_context *ctx, mcg_batch_state *B, mcg_batch_launc
   P.q_log2 = ctx->log2_scale;
   P.refill_steps = ctx->refill;
   P.max_steps = ctx->max_steps;
-  P.cross_margin = 1.0f + ctx->cheap_log_relerr + 0x1p-21f;
   const int tm = B->tally_mode;
   L.smem = sizeof(mcg_libm_tab) + 16 * 8 + 4 * 8 +
            (tm == MCG_TALLY_GLOBAL ? 0 : (size_t)B->max_cells * 8);
@@ -512,7 +510,6 @@ extern "C" int mcg_batch_run_per_slab(mcg_context *ctx)
     P.refill_steps = ctx->refill;
     P.chunk = 64;
     P.max_steps = ctx->max_steps;
-    P.cross_margin = 1.0f + ctx->cheap_log_relerr + 0x1p-21f;
     const int block = ((size_t)sl.n_cells * 64 <= 24 * 1024) ? 256 : 1024;
     const int warps = block / 32;
     const int copies = ((size_t)sl.n_cells * 8 * warps <= 24 * 1024) ? warps : 1;

@@ -30,10 +30,9 @@ struct mcg_libm_dev {
   float tau_log_max, tau_exp_max;
 };
 
-/* RN((float)s) * 2^-63 for s < 2^63 with integer operations only: the
- * hardware 64-bit integer-to-float conversion issues on the FP64 pipe, which
- * GB300 provides at a small fraction of the FP32 rate.  Round to nearest,
- * ties to even, as the reference's (float)seed (src/random.cpp:15). */
+/* RN((float)s) * 2^-63 for s < 2^63 with integer operations only (the
+ * alternative to the hardware conversion, see mcg_rnd_real).  Round to
+ * nearest, ties to even, as the reference's (float)seed (src/random.cpp:15). */
 __device__ __forceinline__ float mcg_u63_unit(uint64_t s)
 {
   if (s == 0)
@@ -50,16 +49,61 @@ __device__ __forceinline__ float mcg_u63_unit(uint64_t s)
 }
 
 /* rnd_real: s <- (G s + C) mod 2^63; h = RN((float)s) * 2^-63.
- * MCG_HW_U2F selects the hardware conversion (FP64 pipe) instead. */
+ * The hardware conversion issues on the FP64 pipe, which the tracker
+ * otherwise leaves idle while its integer/logic pipe is the busiest (measured
+ * +31 % steps/s over mcg_u63_unit); MCG_INT_CONVERSIONS selects the integer
+ * version (same bits). */
 __device__ __forceinline__ float mcg_rnd_real(uint64_t &s)
 {
   s = (MCG_RNG_G * s + MCG_RNG_C) & MCG_MASK63;
-#ifdef MCG_HW_U2F
-  return __fmul_rn(__ull2float_rn(s), 0x1p-63f);
-#else
+#ifdef MCG_INT_CONVERSIONS
   return mcg_u63_unit(s);
+#else
+  return __fmul_rn(__ull2float_rn(s), 0x1p-63f);
 #endif
 }
+
+/* Fast arithmetic's uniform: the same LCG step, then the state's top 23
+ * bits as a float in [0, 1) through the 2^23 bias (two integer/float
+ * operations instead of an exact 64-bit rounding). */
+__device__ __forceinline__ float mcg_rnd_real_fast(uint64_t &s)
+{
+  s = (MCG_RNG_G * s + MCG_RNG_C) & MCG_MASK63;
+  return __uint_as_float(0x3f800000u | (uint32_t)(s >> 40)) - 1.0f;
+}
+
+/* Hardware 2^x (one MUFU operation; subnormal results flush to zero). */
+__device__ __forceinline__ float mcg_ex2_approx(float x)
+{
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+/* Certain-crossing test of the strict tracker.  The reference samples
+ * di = RN(-logf(h) / sig_i) and crosses when !(di < de).  The tracker first
+ * tests  h < E,  E = RN(ex2(RN(RN(sig_i de) * -log2(e))) * MCG_CROSS_FACTOR),
+ * and only evaluates the exact logarithm when the test fails.
+ *
+ * Why h < E implies the crossing (T = sig_i de exactly, u = 2^-24):
+ *  - the two roundings and RN(log2 e) give an exponent T log2(e) (1 + eps)
+ *    with |eps| <= 3.01 u, so 2^exponent lies within a factor
+ *    exp(+-T |eps|) of e^-T;
+ *  - ex2.approx is at most 2^-20 above 2^x (exhaustively checked over every
+ *    argument the test can see by the GPU tests); the last product adds u;
+ *  - h >= 2^-63 when nonzero, so h < E forces T < 44;
+ *  - hence -ln h > T + m - 2^-20 - u - m^2 - 44 |eps|, m = 1 - FACTOR = 2^-14,
+ *    and with the host logf within rho = 2^-22 relative of ln (verified
+ *    exhaustively when the exception table is built):
+ *    -logf(h) >= -ln(h) (1 - rho) > T + m - 2^-20 - u - m^2 - 44 (|eps| + rho) > T,
+ *    so the exact quotient -logf(h) / sig_i is at least de and its rounding,
+ *    RN being monotonic and de a float, is too;
+ *  - h == 0 gives -logf(0) = inf, a crossing for the reference as well.
+ * A false result only costs the exact evaluation: the exact path decides
+ * every case the test does not settle (about 2e-5 of crossings). */
+#define MCG_LOG2E_F 1.44269502f
+#define MCG_CROSS_FACTOR 0.99993896484375f /* 1 - 2^-14 */
+#define MCG_LOGF_RELERR_MAX 0x1p-22f       /* rho above, checked at table load */
 
 __device__ __forceinline__ uint64_t mcg_rnd_seed(uint64_t &s)
 {
@@ -178,13 +222,14 @@ __device__ __forceinline__ float mcg_one_minus_exp_fast(float t)
   return 1.0f - __expf(t);
 }
 
-/* Fixed-point deposit llrint(dw * 2^S), ties to even, with integer
- * operations only (the hardware float-to-int64 conversion issues on the
- * FP64 pipe).  Requires |dw| * 2^S < 2^63. */
+/* Fixed-point deposit llrint(dw * 2^S), ties to even.  By default the
+ * hardware conversion; with MCG_INT_CONVERSIONS the integer version below
+ * (identical results).  Requires |dw| * 2^S < 2^63. */
 __device__ __forceinline__ long long mcg_to_fixed(float dw, int S)
 {
-#ifdef MCG_HW_F2I
-  /* hardware conversion (FP64 pipe); dw * 2^S is exact */
+#ifndef MCG_INT_CONVERSIONS
+  /* hardware conversion on the FP64 pipe (see mcg_rnd_real); dw * 2^S is
+   * exact, and |dw| 2^S < 2^63 is the tally's range */
   return __float2ll_rn(__fmul_rn(dw, __int_as_float((127 + S) << 23)));
 #endif
   const uint32_t u = __float_as_uint(dw);

@@ -40,7 +40,6 @@ struct mcg_event_params {
   uint32_t max_steps;
   mcg_libm_dev libm;
   const mcg_libm_tab *libm_tab;
-  float cross_margin;
 };
 
 /* Fill the first SoA buffer from AoS particles or from the source. */
@@ -80,7 +79,7 @@ __global__ void __launch_bounds__(256) mcg_event_pass_kernel(mcg_event_params P)
   __syncthreads();
   const unsigned n = *P.n_in;
   const int lo = P.cell_lo, hi = P.cell_lo + P.n_cells;
-  const float min_w = P.min_w, cross_margin = P.cross_margin;
+  const float min_w = P.min_w;
   const int qs = P.q_log2;
   unsigned long long tot_steps = 0, tot_scat = 0;
   const unsigned n4 = (n + 3) / 4;
@@ -145,7 +144,7 @@ __global__ void __launch_bounds__(256) mcg_event_pass_kernel(mcg_event_params P)
         }
         mcg_step<STRICT, MCG_TALLY_GLOBAL>(seed[j], x[j], mu[j], wmc[j], inv_mu, idx[j], sc,
                                            __ldg(P.cells + (idx[j] - lo)), &P.tally[idx[j] - lo],
-                                           qs, &T, P.libm, cross_margin);
+                                           qs, &T, P.libm);
         ++nst[j];
       }
       tot_steps += (unsigned long long)(nst[j] - st0);
@@ -300,7 +299,6 @@ int mcg_event_run(mcg_context *ctx, mcg_track_params &TP)
   P.max_steps = TP.max_steps;
   P.libm = TP.libm;
   P.libm_tab = TP.libm_tab;
-  P.cross_margin = TP.cross_margin;
   const int grid_init = (int)std::min<int64_t>((TP.n + 255) / 256, (int64_t)ctx->sm_count * 16);
   cudaEventRecord(ctx->ev0, ctx->stream);
   mcg_event_init_kernel<<<grid_init, 256, 0, ctx->stream>>>(TP, ctx->event_buf[0], ctx->event_count);

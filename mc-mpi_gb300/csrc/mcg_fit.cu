@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(512) mcg_fit_kernel(mcg_fit_params P)
         bool coll;
         mcg_step<false, MCG_TALLY_SMEM32>(seed, x, mu, wmc, inv_mu, idx, nsc, cells[c],
                                           phase == 0 ? &s_tally[c] : nullptr, P.q_log2, nullptr,
-                                          no_libm, 1.0f, &l, &coll, &dep);
+                                          no_libm, &l, &coll, &dep);
         const float g = __fmul_rn(wc, dep);
         if (phase == 0) {
           fit_ff_add(G_hi, G_lo, g);
@@ -262,29 +262,26 @@ struct mcg_fit_state {
   float min_w = 0.f;
 };
 
-static std::vector<std::pair<mcg_context *, mcg_fit_state *>> g_fit;
-
 static mcg_fit_state *fit_of(mcg_context *ctx, bool create)
 {
-  for (auto &p : g_fit)
-    if (p.first == ctx)
-      return p.second;
-  if (!create)
-    return nullptr;
-  g_fit.push_back({ctx, new mcg_fit_state()});
-  return g_fit.back().second;
+  if (!ctx->ext) {
+    if (!create)
+      return nullptr;
+    ctx->ext = new mcg_ext();
+  }
+  if (!ctx->ext->fit && create)
+    ctx->ext->fit = new mcg_fit_state();
+  return ctx->ext->fit;
 }
 
 extern "C" int mcg_fit_release(mcg_context *ctx)
 {
-  for (size_t i = 0; i < g_fit.size(); ++i)
-    if (g_fit[i].first == ctx) {
-      if (g_fit[i].second->dev)
-        cudaFree(g_fit[i].second->dev);
-      delete g_fit[i].second;
-      g_fit.erase(g_fit.begin() + i);
-      return MCG_OK;
-    }
+  if (!ctx || !ctx->ext || !ctx->ext->fit)
+    return MCG_OK;
+  if (ctx->ext->fit->dev)
+    cudaFree(ctx->ext->fit->dev);
+  delete ctx->ext->fit;
+  ctx->ext->fit = nullptr;
   return MCG_OK;
 }
 

@@ -45,9 +45,12 @@ struct mcg_adj_state {
   int g_log2 = 36;
 };
 
+struct mcg_fit_state; /* mcg_fit.cu */
+
 struct mcg_ext {
   mcg_batch_state batch;
   mcg_adj_state adj;
+  mcg_fit_state *fit = nullptr;
 };
 
 /* Structure-of-arrays particle buffer of the event-based tracker. */
@@ -82,7 +85,6 @@ struct mcg_context {
   mcg_libm_dev libm = {};
   mcg_libm_tab *libm_tab = nullptr;
   uint32_t libm_n_log = 0, libm_n_exp = 0;
-  float cheap_log_relerr = 1e-3f; /* replaced by the table's measured bound */
 
   /* particle buffers of the host-pointer entry points */
   mcg_particle *d_part = nullptr;

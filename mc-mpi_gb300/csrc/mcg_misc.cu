@@ -28,6 +28,8 @@ __global__ void mcg_libm_eval_kernel(int fn, const float *in, float *out, int64_
     float v = in[i], r;
     if (fn == 0)
       r = (v >= 0.0f && v <= 1.0f) ? mcg_logf_strict(v, &T, L) : __int_as_float(0x7fc00000);
+    else if (fn == 2)
+      r = mcg_ex2_approx(v);
     else
       r = (v >= MCG_EXP_ONE_BOUND && v < 89.0f) ? mcg_expf_strict(v, &T, L)
                                                 : __int_as_float(0x7fc00000);
@@ -53,7 +55,7 @@ extern "C" int mcg_rnd_real_device(mcg_context *ctx, uint64_t *d_seeds, float *d
 extern "C" int mcg_libm_eval_device(mcg_context *ctx, int fn, const float *d_in, float *d_out,
                                     int64_t n)
 {
-  if (!ctx || (fn != 0 && fn != 1) || n < 0 || (n > 0 && (!d_in || !d_out)))
+  if (!ctx || fn < 0 || fn > 2 || n < 0 || (n > 0 && (!d_in || !d_out)))
     return mcg_fail(MCG_ERR_ARG, "mcg_libm_eval_device: bad arguments");
   if (!ctx->libm_loaded)
     return mcg_fail(MCG_ERR_STATE, "mcg_libm_eval_device: needs a strict context");

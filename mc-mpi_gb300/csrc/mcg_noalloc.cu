@@ -120,7 +120,6 @@ extern "C" int mcg_simulate_fast_noalloc(int n_layers, const int32_t *h_index_st
     P.refill_steps = 8;
     P.chunk = 64;
     P.max_steps = 1u << 28;
-    P.cross_margin = 1.0f;
     const int block = ((size_t)total * 8 * 8 <= 24 * 1024) ? 256 : 1024;
     const int warps = block / 32;
     const int copies = ((size_t)total * 8 * warps <= 24 * 1024) ? warps : 1;

@@ -43,7 +43,6 @@ struct mcg_track_params {
   int32_t tally_copies; /* 1 or warps per block */
   int32_t chunk;        /* histories per warp grab (multiple of 32) */
   uint32_t max_steps;
-  float cross_margin;   /* 1 + relative margin of the certain-crossing test */
 };
 
 /* Tally accumulation: shared-memory 64-bit atomics, shared-memory 32-bit
@@ -111,17 +110,18 @@ __device__ __forceinline__ void mcg_load_particle(const mcg_track_params &P, int
  * cell c = {sig_a, sig_i or -ln2/sig_i, edge_lo, edge_hi}; deposits into
  * *tally_cell.  STRICT: the reference's float operations and host-libm
  * logf/expf; the crossing's absorption is computed before the logarithm and
- * a certified cheap log settles most crossings.  FAST: hardware log2/exp2. */
+ * a certified exponential bound settles most crossings without it (see
+ * MCG_CROSS_FACTOR).  FAST: hardware log2/exp2. */
 template <bool STRICT, int TALLY>
 __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, float &wmc,
                                          float &inv_mu, int &idx, uint32_t &nsc, const float4 c,
                                          unsigned long long *tally_cell, int qs,
                                          const mcg_libm_tab *T, const mcg_libm_dev &LM,
-                                         float cross_margin, float *l_out = nullptr,
+                                         float *l_out = nullptr,
                                          bool *coll_out = nullptr, float *dep_out = nullptr)
 {
   const float sig_a = c.x;
-  const float h = mcg_rnd_real(seed);
+  const float h = STRICT ? mcg_rnd_real(seed) : mcg_rnd_real_fast(seed);
   const bool neg = mu < 0.0f;
   int inew = neg ? idx - 1 : idx + 1;
   const float edge = neg ? c.z : c.w;
@@ -133,15 +133,14 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
         (mu < -MCG_EPS || MCG_EPS < mu) ? __fdiv_rn(__fsub_rn(edge, x), mu) : MCG_MAXREAL;
     const float om_cross = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, de), T, LM);
     /* di = sig_i > EPS ? -log(h) / sig_i : MAXREAL; the exact value is
-     * only needed when the flight may end inside the cell: a cheap
-     * -log with a certified margin settles most crossings */
+     * only needed when the flight may end inside the cell: the certified
+     * test h < ~exp(-sig_i de) settles almost every crossing */
     bool cross;
     float di = MCG_MAXREAL;
     if (c.y > MCG_EPS) {
-      const bool sure = h > 0.0f && c.y < 1e30f &&
-                        __fmul_rn(mcg_neglog_cheap(h, T), __frcp_rn(c.y)) >
-                            __fmul_rn(de, cross_margin);
-      if (sure) {
+      const float bound = __fmul_rn(
+          mcg_ex2_approx(__fmul_rn(__fmul_rn(c.y, de), -MCG_LOG2E_F)), MCG_CROSS_FACTOR);
+      if (h < bound) {
         cross = true;
       } else {
         di = __fdiv_rn(-mcg_logf_strict(h, T, LM), c.y);
@@ -181,7 +180,7 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
     if (coll) {
       inew = idx;
       x = fmaf(di, mu, x);
-      mu = fmaf(2.0f, mcg_rnd_real(seed), -1.0f);
+      mu = fmaf(2.0f, mcg_rnd_real_fast(seed), -1.0f);
       inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
       om = mcg_one_minus_exp_fast(-sig_a * di);
       ++nsc;
@@ -228,7 +227,6 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
   unsigned long long *my_tally = TALLY == MCG_TALLY_GLOBAL
                                      ? P.tally
                                      : s_tally + (size_t)(warp % P.tally_copies) * ncell;
-  const float cross_margin = P.cross_margin;
 
   uint64_t seed = 0;
   float x = 0.f, mu = 0.f, wmc = 0.f, inv_mu = 0.f;
@@ -330,7 +328,7 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
         break;
       }
       mcg_step<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + (idx - lo)),
-                              &my_tally[idx - lo], qs, T, P.libm, cross_margin);
+                              &my_tally[idx - lo], qs, T, P.libm);
       ++nst;
     }
   }

@@ -50,7 +50,6 @@ struct mcg_worker_params {
   unsigned long long *tally, *counters, *done, *handoffs;
   mcg_libm_dev libm;
   const mcg_libm_tab *libm_tab;
-  float cross_margin;
   uint32_t max_steps;
 };
 
@@ -117,7 +116,7 @@ __global__ void __launch_bounds__(256) mcg_worker_cycle(mcg_worker_params P, int
       /* Layer::simulate_particle within this sub-domain */
       while ((wmc >= min_w) && (idx < hi) && (idx >= lo) && nst < P.max_steps) {
         mcg_step<STRICT, MCG_TALLY_SMEM32>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(cells + (idx - lo)),
-                                           &s_tally[idx - lo], P.q_log2, T, P.libm, P.cross_margin);
+                                           &s_tally[idx - lo], P.q_log2, T, P.libm);
         ++nst;
       }
       steps += nst;
@@ -248,7 +247,6 @@ extern "C" int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n
   W.handoffs = cnt + 2;
   W.libm = ctx->libm;
   W.libm_tab = ctx->libm_tab;
-  W.cross_margin = 1.0f + ctx->cheap_log_relerr + 0x1p-21f;
   W.max_steps = ctx->max_steps;
   const int bpl = std::max(1, std::min(8, (int)((per_cycle + 255) / 256)));
   auto kern = strict ? mcg_worker_cycle<true> : mcg_worker_cycle<false>;

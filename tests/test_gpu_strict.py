@@ -155,6 +155,7 @@ def test_rnd_real_device_kat(ctx, oracle):
     g = load("rng_chain.npz")
     seeds = torch.tensor(g["seeds"].view(np.int64), device="cuda")
     reals = torch.empty(len(g["seeds"]), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()  # the library runs on its own stream
     ctx.rnd_real_device(seeds.data_ptr(), reals.data_ptr(), len(g["seeds"]))
     assert np.array_equal(seeds.cpu().numpy().view(np.uint64), g["seeds_after"])
     assert np.array_equal(reals.cpu().numpy().view(np.uint32), g["reals"].view(np.uint32))
@@ -186,6 +187,35 @@ def test_strict_libm_exhaustive(ctx, oracle, fn):
             host = oracle.libm_array(fn, x).view(np.uint32)
             bad += int(np.count_nonzero(gpu != host))
     assert bad == 0
+
+
+def test_cross_bound_ex2_exhaustive(ctx):
+    """The strict tracker's certain-crossing test assumes the hardware 2^x
+    never exceeds the exact value by more than 2^-20 relative.  Checked for
+    every float argument in [-150, 0] (below, the result must be 0)."""
+    import torch
+    chunk = 1 << 26
+    worst = 0.0
+    a, b = 0x80000000, int(np.array([-150.0], np.float32).view(np.uint32)[0]) + 1
+    for s in range(a, b, chunk):
+        e = min(s + chunk, b)
+        u = torch.arange(s, e, dtype=torch.int64, device="cuda")
+        x = (u - (1 << 32)).to(torch.int32).view(torch.float32)
+        out = torch.empty_like(x)
+        torch.cuda.synchronize()  # the library runs on its own stream
+        ctx.libm_eval_device(2, x.data_ptr(), out.data_ptr(), x.numel())
+        exact = torch.exp2(x.double())
+        rel = (out.double() - exact) / exact
+        worst = max(worst, float(rel.max()))
+    assert worst <= 2.0 ** -20, worst
+    # arguments below -150 (every 4099th float, and -inf) give 0
+    u = torch.arange(b, 0xFF800001, 4099, dtype=torch.int64, device="cuda")
+    u = torch.cat([u, torch.tensor([0xFF800000], dtype=torch.int64, device="cuda")])
+    x = (u - (1 << 32)).to(torch.int32).view(torch.float32)
+    out = torch.empty_like(x)
+    torch.cuda.synchronize()
+    ctx.libm_eval_device(2, x.data_ptr(), out.data_ptr(), x.numel())
+    assert float(out.max()) == 0.0
 
 
 def _slab(mcg, nb, P):
