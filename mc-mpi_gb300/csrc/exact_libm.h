@@ -161,20 +161,18 @@ MCG_HD float mcg_exp_ff(float t, float *delta, const mcg_libm_tab *T)
   if (!(t < 89.0f)) { *delta = 0.5f; return mcg_u2f(0x7f800000u); }
   int k = mcg_rint_k(MCG_MUL(t, MCG_EXP_INV));
   if (k == 0) {
-    /* |t| <= ln2/128: the general path below with every k-term zero and
-     * T = 1 (identical bits, fewer operations) */
-    float q2h = MCG_MUL(t, t);
-    float q2l = MCG_FMA(t, t, -q2h);
-    float h2h = MCG_MUL(0.5f, q2h);
-    float sh = MCG_ADD(t, h2h);
-    float sl = MCG_ADD(MCG_SUB(t, sh), h2h);
-    float Q = MCG_FMA(t, MCG_FMA(t, MCG_EXP_Q5, MCG_EXP_Q4), MCG_EXP_Q3);
-    sl = MCG_ADD(sl, MCG_ADD(MCG_MUL(0.5f, q2l), MCG_MUL(MCG_MUL(q2h, t), Q)));
-    float z = MCG_ADD(1.0f, sh);
-    float ze = MCG_ADD(MCG_SUB(1.0f, z), sh);
-    float lo = MCG_ADD(ze, sl);
-    float yh = MCG_ADD(z, lo);
-    float yl = MCG_ADD(MCG_SUB(z, yh), lo);
+    /* |t| <= ln2/128: e^t = (1 + t) + t^2 (1/2 + t/6 + t^2/24), the first
+     * sum exact as a float-float (Fast2Sum), the tail within 2^-38.  Less
+     * accurate than the general path, which the exception table absorbs:
+     * its generator runs this same code over every argument. */
+    float p = MCG_FMA(t, MCG_EXP_Q4, MCG_EXP_Q3);
+    p = MCG_FMA(t, p, 0.5f);
+    float r2 = MCG_MUL(MCG_MUL(t, t), p);
+    float s = MCG_ADD(1.0f, t);
+    float se = MCG_SUB(t, MCG_SUB(s, 1.0f));
+    float lo = MCG_ADD(se, r2);
+    float yh = MCG_ADD(s, lo);
+    float yl = MCG_ADD(MCG_SUB(s, yh), lo);
     /* mcg_midpoint_delta for yh in [0.99, 1.01]: the spacing on yl's side is
      * 2^-24 below 1 (and below 1.0 itself), 2^-23 from 1 up */
     const uint32_t ub = mcg_f2u(yh);

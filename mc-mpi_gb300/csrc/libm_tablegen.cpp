@@ -50,7 +50,7 @@ int main(int argc, char **argv)
     mcg_libm_file h;
     FILE *fp = fopen(argv[2], "rb");
     bool ok = fp && fread(&h, sizeof(h), 1, fp) == 1 && memcmp(h.magic, MCG_LIBM_MAGIC, 8) == 0 &&
-              h.fingerprint == mcg_libm_fingerprint();
+              h.fingerprint == mcg_libm_fingerprint(&kTab);
     if (fp)
       fclose(fp);
     return ok ? 0 : 1;
@@ -109,7 +109,7 @@ int main(int argc, char **argv)
   memset(&f, 0, sizeof(f));
   memcpy(f.magic, MCG_LIBM_MAGIC, 8);
   snprintf(f.libc_version, sizeof(f.libc_version), "glibc %s", gnu_get_libc_version());
-  f.fingerprint = mcg_libm_fingerprint();
+  f.fingerprint = mcg_libm_fingerprint(&kTab);
   std::vector<uint32_t> pairs[2];
   for (int fn = 0; fn < 2; ++fn) {
     std::vector<Exc> all;

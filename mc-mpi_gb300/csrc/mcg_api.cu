@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "exact_libm.h"
 #include "libm_file.h"
 #include "mcg_internal.h"
 #include "mcg_track.cuh"
@@ -99,9 +100,11 @@ int mcg_load_libm(mcg_context *ctx)
   fclose(f);
   if (!ok)
     return mcg_fail(MCG_ERR_TABLES, "malformed libm exception table %s", path.c_str());
-  if (hdr.fingerprint != mcg_libm_fingerprint())
+  const mcg_libm_tab tab = MCG_LIBM_TAB_INIT;
+  if (hdr.fingerprint != mcg_libm_fingerprint(&tab))
     return mcg_fail(MCG_ERR_TABLES,
-                    "libm exception table %s was made against another C library (%s); rebuild",
+                    "libm exception table %s was made against another C library (%s) or "
+                    "another version of the evaluators; rebuild",
                     path.c_str(), hdr.libc_version);
   if (!(hdr.logf_relerr <= MCG_LOGF_RELERR_MAX))
     return mcg_fail(MCG_ERR_TABLES,
@@ -121,7 +124,6 @@ int mcg_load_libm(mcg_context *ctx)
   }
   ctx->libm.tau_log_max = tl;
   ctx->libm.tau_exp_max = te;
-  const mcg_libm_tab tab = MCG_LIBM_TAB_INIT;
   cudaError_t e;
   float *dtl, *dte;
   uint2 *dhl, *dhe;
