@@ -8,8 +8,9 @@ sigma_s(x) = 2.0 + 1.5 cos(4 pi x) at cell centres (fp32), particles born at
 x = 0, mu = 1, weight 1.0, seeds from the reference's rnd_seed chain started
 at 5127801, minimum weight 1e-12 (implicit capture, as Layer::simulate).
 The full problem is 1e8 histories; one bench step runs one batch of
---batch consecutive histories of that source (default 1e7, so 10 steps
-cover the whole 1e8).  Synthetic data: the reference has no dataset.
+--batch consecutive histories of that source (default: all 1e8 in one
+launch, so the launch's tail, where the SMs wait on the longest histories,
+is paid once per 1e8).  Synthetic data: the reference has no dataset.
 
 batched / adjoint : the metric's other two forms (batched slabs of
         configuration 2, forward+adjoint of configuration 3), each timed with
@@ -215,11 +216,18 @@ def run_gpu(args):
     def batch_first(k):
         return (rank * (args.warmup + args.steps) + k) * B % N_TOTAL
 
+    built = [None]
+
     def make_batch(k):
+        """Born particles of step k in the pinned host buffer (rebuilt only
+        when the step's histories differ from the buffer's)."""
+        if built[0] == batch_first(k):
+            return
         arr = np.frombuffer(host_p.numpy(), dtype=mcg.PARTICLE_DTYPE)
         src = mcg.Source(0, 0, BASE_SEED, 0.0, 1.0, 1.0, 0)
         mcg._check(mcg.load_library().mcg_create_particles(
             ctx.h, C.byref(src), batch_first(k), B, arr.ctypes.data_as(C.c_void_p)))
+        built[0] = batch_first(k)
 
     def device_step(k):
         make_batch(k)
@@ -261,6 +269,7 @@ def run_gpu(args):
                                     C.c_void_p(host_r.data_ptr()), None, None))
         tq = ctx.tally_q()
         e2e_times.append(time.perf_counter() - t1)
+        built[0] = None  # the call wrote the final particle states back
     e2e_s = statistics.median(e2e_times[1:])
     e2e_val = B / e2e_s
 
@@ -301,6 +310,25 @@ def run_gpu(args):
                            "peak_gops": sms * 128 * f_sm / 1e9, "frac": issue_frac},
         "clocks": clocks,
     }
+    if rank == 0 and not args.no_extra and args.mode == "strict":
+        # the same steps with fast arithmetic (hardware log2/exp2; tallies
+        # statistically equivalent, not bit-identical)
+        fctx = mcg.Context(mode="fast", device=local)
+        fctx.set_layers(st, m, dx, sigs, rates, MIN_W)
+        fctx.set_tally_scale(35)
+        fms = []
+        for k in range(3):
+            make_batch(args.warmup)
+            part.copy_(host_p, non_blocking=False)
+            flush.zero_()
+            torch.cuda.synchronize()
+            fctx.simulate_device_ptr(part.data_ptr(), B, res.data_ptr())
+            fms.append(fctx.last_kernel_ms())
+        fc = fctx.counters()
+        line["fast"] = {"value": B / (statistics.median(fms[1:]) / 1e3), "unit": "histories/s",
+                        "warmup": 1, "steps": 2,
+                        "steps_per_s": fc["steps"] / (sum(fms) / 1e3)}
+        fctx.close()
     if rank == 0 and not args.no_extra:
         line["batched"] = bench_batched(mcg, args.mode, local)
         line["adjoint"] = bench_adjoint(mcg, args.mode, local)
@@ -464,7 +492,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="strict", choices=["strict", "fast"])
-    ap.add_argument("--batch", type=int, default=10_000_000)
+    ap.add_argument("--batch", type=int, default=N_TOTAL)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="plain", choices=["plain", "batch", "adjoint", "fit"])
     ap.add_argument("--scale", type=float, default=1.0,

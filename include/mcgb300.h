@@ -320,6 +320,14 @@ int mcg_rnd_real_device(mcg_context *ctx, uint64_t *d_seeds, float *d_reals, int
  * hardware 2^x of the strict tracker's certain-crossing test. */
 int mcg_libm_eval_device(mcg_context *ctx, int fn, const float *d_in, float *d_out, int64_t n);
 
+/* Check of the strict tracker's division by a cached reciprocal against the
+ * IEEE quotient (testing aid): mode 0 every pair of significands (2^46
+ * pairs, about half a minute), mode 1 n pseudo-random pairs over the
+ * tracker's exponent range.  Returns the pairs checked, the mismatches and
+ * one mismatching pair's bits (a << 32 | b, 0 if none). */
+int mcg_verify_division(mcg_context *ctx, int mode, uint64_t n, uint64_t *checked,
+                        uint64_t *mismatches, uint64_t *example);
+
 #ifdef __cplusplus
 }
 #endif

@@ -119,6 +119,7 @@ def load_library(path=None):
         "mcg_batch_set_launch": (C.c_int, [vp, i32, i64, i32]),
         "mcg_batch_autotune": (C.c_int, [vp, C.c_double, C.POINTER(Tuning)]),
         "mcg_libm_eval_device": (C.c_int, [vp, C.c_int, vp, vp, i64]),
+        "mcg_verify_division": (C.c_int, [vp, C.c_int, C.c_uint64] + [C.POINTER(C.c_uint64)] * 3),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -392,6 +393,13 @@ class Context:
     def rnd_real_device(self, d_seeds, d_reals, n):
         _device_inputs_ready()
         _check(self.lib.mcg_rnd_real_device(self.h, C.c_void_p(d_seeds), C.c_void_p(d_reals), n))
+
+    def verify_division(self, mode, n=0):
+        """(pairs checked, mismatches, one mismatching pair's bits) of the
+        cached-reciprocal division against the IEEE quotient."""
+        c, m, x = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(self.lib.mcg_verify_division(self.h, mode, n, C.byref(c), C.byref(m), C.byref(x)))
+        return c.value, m.value, x.value
 
     def libm_eval_device(self, fn, d_in, d_out, n):
         _device_inputs_ready()

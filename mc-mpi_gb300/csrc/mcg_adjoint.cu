@@ -125,8 +125,7 @@ __global__ void __launch_bounds__(1024) mcg_adjoint_kernel(mcg_adj_params P)
       if (!active && my >= 0) {
         hid = my;
         mcg_source_particle(P.src, P.first + hid, seed, x, mu, wmc, idx);
-        if (!STRICT)
-          inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
+        inv_mu = mcg_flight_rcp(mu);
         nst = nsc = 0;
         phase = 0;
         G_hi = G_lo = P_hi = P_lo = 0.f;
@@ -147,8 +146,7 @@ __global__ void __launch_bounds__(1024) mcg_adjoint_kernel(mcg_adj_params P)
           tot_steps += nst;
           tot_scat += nsc;
           mcg_source_particle(P.src, P.first + hid, seed, x, mu, wmc, idx);
-          if (!STRICT)
-            inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
+          inv_mu = mcg_flight_rcp(mu);
           nst = nsc = 0;
           phase = 1;
           continue;

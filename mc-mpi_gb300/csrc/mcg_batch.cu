@@ -140,8 +140,7 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
         }
         if (!active && my >= 0) {
           mcg_source_particle(S, it.first + my, seed, x, mu, wmc, idx);
-          if (!STRICT)
-            inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
+          inv_mu = mcg_flight_rcp(mu);
           nst = nsc = 0;
           active = true;
         }

@@ -72,6 +72,25 @@ __device__ __forceinline__ float mcg_rnd_real_fast(uint64_t &s)
   return __uint_as_float(0x3f800000u | (uint32_t)(s >> 40)) - 1.0f;
 }
 
+/* RN(1 / mu) of a flight, 0 when |mu| <= EPS (the reference then uses
+ * d_edge = MAXREAL, src/layer.cpp:159). */
+__device__ __forceinline__ float mcg_flight_rcp(float mu)
+{
+  return (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
+}
+
+/* RN(a / b) from y = RN(1 / b): q = RN(a y), r = a - b q (exact by fma),
+ * q + r y rounded once.  Equal to the IEEE quotient for every pair of
+ * significands (checked exhaustively, all 2^46 pairs, by the GPU tests
+ * through mcg_verify_division); each operation commutes with scaling a and
+ * b by powers of two while no intermediate leaves the normal range, which
+ * the caller guarantees by |a| >= 2^-100, 2^-100 <= |b| <= 2^100. */
+__device__ __forceinline__ float mcg_div_by_rcp(float a, float b, float y)
+{
+  const float q = __fmul_rn(a, y);
+  return __fmaf_rn(__fmaf_rn(-b, q, a), y, q);
+}
+
 /* Hardware 2^x (one MUFU operation; subnormal results flush to zero). */
 __device__ __forceinline__ float mcg_ex2_approx(float x)
 {

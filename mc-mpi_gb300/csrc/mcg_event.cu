@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(256) mcg_event_pass_kernel(mcg_event_params P)
     for (int j = 0; j < 4; ++j) {
       if (!live[j])
         continue;
-      float inv_mu = (mu[j] < -MCG_EPS || MCG_EPS < mu[j]) ? __frcp_rn(mu[j]) : 0.0f;
+      float inv_mu = mcg_flight_rcp(mu[j]);
       uint32_t sc = (uint32_t)nsc[j];
       const int st0 = nst[j];
       for (int k = 0; k < P.steps_per_pass; ++k) {

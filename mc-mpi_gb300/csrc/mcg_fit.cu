@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(512) mcg_fit_kernel(mcg_fit_params P)
         if (!active && my >= 0) {
           my_h = my;
           mcg_source_particle(sd.src, src_base + my_h, seed, x, mu, wmc, idx);
-          inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
+          inv_mu = mcg_flight_rcp(mu);
           nst = nsc = 0;
           phase = 0;
           G_hi = G_lo = P_hi = P_lo = 0.f;
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(512) mcg_fit_kernel(mcg_fit_params P)
         if (!((wmc >= P.min_w) && (idx < m) && (idx >= 0)) || nst >= P.max_steps) {
           if (phase == 0 && P.with_grad) {
             mcg_source_particle(sd.src, src_base + my_h, seed, x, mu, wmc, idx);
-            inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
+            inv_mu = mcg_flight_rcp(mu);
             nst = nsc = 0;
             phase = 1;
             continue;

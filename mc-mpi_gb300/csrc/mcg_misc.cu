@@ -1,7 +1,8 @@
 /*
  * mcg_misc.cu - small device entry points: the reference's rnd_real kernel
- * (src/curandom.cu:7-14) and an evaluator of the strict libm, used to check
- * the device arithmetic against the host C library exhaustively.
+ * (src/curandom.cu:7-14), an evaluator of the strict libm, used to check
+ * the device arithmetic against the host C library exhaustively, and the
+ * check of the tracker's division by a cached reciprocal.
  */
 #include "mcg_internal.h"
 
@@ -68,4 +69,87 @@ extern "C" int mcg_libm_eval_device(mcg_context *ctx, int fn, const float *d_in,
   if (e == cudaSuccess)
     e = cudaStreamSynchronize(ctx->stream);
   return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(e, "mcg_libm_eval_device");
+}
+
+/* Checks mcg_div_by_rcp against the IEEE quotient.  mode 0: every pair of
+ * significands a, b in [1, 2) (b from b_first, b_count of them); mode 1: n
+ * pseudo-random pairs of either sign, |a| in [2^-100, 4), |b| in
+ * [2^-14, 1).  out[0] += pairs checked, out[1] += mismatches,
+ * out[2] = bits of one mismatching pair (a << 32 | b) if any. */
+__global__ void mcg_verify_div_kernel(int mode, uint32_t b_first, uint32_t b_count, uint64_t n,
+                                      unsigned long long *out)
+{
+  unsigned long long checked = 0, bad = 0;
+  if (mode == 0) {
+    for (uint32_t jb = b_first + blockIdx.x; jb < b_first + b_count; jb += gridDim.x) {
+      const float b = __uint_as_float(0x3f800000u | jb), y = __frcp_rn(b);
+      for (uint32_t ia = threadIdx.x; ia < (1u << 23); ia += blockDim.x) {
+        const float a = __uint_as_float(0x3f800000u | ia);
+        const float q = mcg_div_by_rcp(a, b, y), ref = __fdiv_rn(a, b);
+        ++checked;
+        if (__float_as_uint(q) != __float_as_uint(ref)) {
+          ++bad;
+          atomicCAS(out + 2, 0ull, ((unsigned long long)__float_as_uint(a) << 32) | __float_as_uint(b));
+        }
+      }
+    }
+  } else {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+      uint64_t h = (i + 1) * 0x9E3779B97F4A7C15ull;
+      h ^= h >> 31;
+      h *= 0xBF58476D1CE4E5B9ull;
+      h ^= h >> 29;
+      const uint32_t u = (uint32_t)h, v = (uint32_t)(h >> 32);
+      const uint32_t ea = 27u + (u >> 8) % 102u, eb = 113u + (v >> 8) % 14u;
+      const float a = __uint_as_float((u & 0x80000000u) | (ea << 23) | ((u * 2654435761u) & 0x7fffffu));
+      const float b = __uint_as_float((v & 0x80000000u) | (eb << 23) | ((v * 2246822519u) & 0x7fffffu));
+      const float q = mcg_div_by_rcp(a, b, __frcp_rn(b)), ref = __fdiv_rn(a, b);
+      ++checked;
+      if (__float_as_uint(q) != __float_as_uint(ref)) {
+        ++bad;
+        atomicCAS(out + 2, 0ull, ((unsigned long long)__float_as_uint(a) << 32) | __float_as_uint(b));
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    checked += __shfl_down_sync(0xffffffffu, checked, o);
+    bad += __shfl_down_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(out, checked);
+    if (bad)
+      atomicAdd(out + 1, bad);
+  }
+}
+
+extern "C" int mcg_verify_division(mcg_context *ctx, int mode, uint64_t n, uint64_t *checked,
+                                   uint64_t *mismatches, uint64_t *example)
+{
+  if (!ctx || (mode != 0 && mode != 1) || !checked || !mismatches || !example)
+    return mcg_fail(MCG_ERR_ARG, "mcg_verify_division: bad arguments");
+  cudaSetDevice(ctx->device);
+  unsigned long long *d = nullptr;
+  cudaError_t e = cudaMalloc(&d, 3 * sizeof(unsigned long long));
+  if (e != cudaSuccess)
+    return mcg_cuda_fail(e, "cudaMalloc(verify)");
+  e = cudaMemsetAsync(d, 0, 3 * sizeof(unsigned long long), ctx->stream);
+  const int grid = ctx->sm_count * 8;
+  /* mode 0 in 64 launches of 2^17 divisors (about half a second each) */
+  for (int part = 0; e == cudaSuccess && part < (mode == 0 ? 64 : 1); ++part) {
+    mcg_verify_div_kernel<<<grid, 256, 0, ctx->stream>>>(mode, (uint32_t)part << 17, 1u << 17, n, d);
+    e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = cudaStreamSynchronize(ctx->stream);
+  }
+  unsigned long long h[3] = {0, 0, 0};
+  if (e == cudaSuccess)
+    e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess)
+    return mcg_cuda_fail(e, "mcg_verify_division");
+  *checked = h[0];
+  *mismatches = h[1];
+  *example = h[2];
+  return MCG_OK;
 }

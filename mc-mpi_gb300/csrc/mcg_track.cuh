@@ -129,8 +129,10 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
   if (STRICT) {
     /* d_edge, and the crossing's absorption, do not depend on the flight
      * sample: start them before the logarithm */
-    const float de =
-        (mu < -MCG_EPS || MCG_EPS < mu) ? __fdiv_rn(__fsub_rn(edge, x), mu) : MCG_MAXREAL;
+    const float a = __fsub_rn(edge, x), aa = fabsf(a);
+    const float de = inv_mu == 0.0f ? MCG_MAXREAL
+                     : (aa >= 0x1p-100f && aa <= 0x1p100f) ? mcg_div_by_rcp(a, mu, inv_mu)
+                                                            : __fdiv_rn(a, mu);
     const float om_cross = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, de), T, LM);
     /* di = sig_i > EPS ? -log(h) / sig_i : MAXREAL; the exact value is
      * only needed when the flight may end inside the cell: the certified
@@ -153,6 +155,7 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
       inew = idx;
       x = __fadd_rn(x, __fmul_rn(di, mu));
       mu = __fsub_rn(__fmul_rn(2.0f, mcg_rnd_real(seed)), 1.0f);
+      inv_mu = mcg_flight_rcp(mu);
       om = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, di), T, LM);
       ++nsc;
     } else {
@@ -181,7 +184,7 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
       inew = idx;
       x = fmaf(di, mu, x);
       mu = fmaf(2.0f, mcg_rnd_real_fast(seed), -1.0f);
-      inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
+      inv_mu = mcg_flight_rcp(mu);
       om = mcg_one_minus_exp_fast(-sig_a * di);
       ++nsc;
     } else {
@@ -269,8 +272,7 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
       if (!active && my >= 0) {
         hid = my;
         mcg_load_particle(P, hid, seed, x, mu, wmc, idx);
-        if (!STRICT)
-          inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
+        inv_mu = mcg_flight_rcp(mu);
         nst = nsc = 0;
         active = true;
       }

@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(256) mcg_worker_cycle(mcg_worker_params P, int
       } else {
         mcg_source_particle(P.src, (int64_t)(src_first + (k - take)), seed, x, mu, wmc, idx);
       }
-      inv_mu = (mu < -MCG_EPS || MCG_EPS < mu) ? __frcp_rn(mu) : 0.0f;
+      inv_mu = mcg_flight_rcp(mu);
       /* Layer::simulate_particle within this sub-domain */
       while ((wmc >= min_w) && (idx < hi) && (idx >= lo) && nst < P.max_steps) {
         mcg_step<STRICT, MCG_TALLY_SMEM32>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(cells + (idx - lo)),

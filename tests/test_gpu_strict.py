@@ -218,6 +218,17 @@ def test_cross_bound_ex2_exhaustive(ctx):
     assert float(out.max()) == 0.0
 
 
+@pytest.mark.parametrize("mode", [0, 1])
+def test_division_by_cached_reciprocal(ctx, mode):
+    """The strict tracker divides by RN(1/mu) cached per flight: equal to the
+    IEEE quotient for all 2^46 significand pairs (mode 0) and for random
+    pairs over the tracker's exponent range (mode 1)."""
+    n = 1 << 30
+    checked, bad, example = ctx.verify_division(mode, n)
+    assert checked == (1 << 46 if mode == 0 else n)
+    assert bad == 0, hex(example)
+
+
 def _slab(mcg, nb, P):
     from mc_mpi_gb300 import workloads
     sigs, rates = workloads.config1(nb)
