@@ -155,10 +155,10 @@ MCG_HD float mcg_log_ff(float x, float *delta, const mcg_libm_tab *T)
   return yh;
 }
 
-/* exp(t) for -17.5 <= t < 89.  Larger t returns +inf with delta 0.5. */
-MCG_HD float mcg_exp_ff(float t, float *delta, const mcg_libm_tab *T)
+/* exp(t) for -17.5 <= t < 89 (other arguments give meaningless values,
+ * and touch nothing outside T). */
+MCG_HD float mcg_exp_ff_core(float t, float *delta, const mcg_libm_tab *T)
 {
-  if (!(t < 89.0f)) { *delta = 0.5f; return mcg_u2f(0x7f800000u); }
   int k = mcg_rint_k(MCG_MUL(t, MCG_EXP_INV));
   if (k == 0) {
     /* |t| <= ln2/128: e^t = (1 + t) + t^2 (1/2 + t/6 + t^2/24), the first
@@ -217,6 +217,13 @@ MCG_HD float mcg_exp_ff(float t, float *delta, const mcg_libm_tab *T)
   /* scale by 2^q, q in [-26, 128]; the product is exact unless it overflows */
   if (q > 127) { yh = MCG_MUL(yh, 2.0f); q -= 1; }
   return MCG_MUL(yh, mcg_u2f((uint32_t)(q + 127) << 23));
+}
+
+/* exp(t) for -17.5 <= t < 89.  Larger t returns +inf with delta 0.5. */
+MCG_HD float mcg_exp_ff(float t, float *delta, const mcg_libm_tab *T)
+{
+  if (!(t < 89.0f)) { *delta = 0.5f; return mcg_u2f(0x7f800000u); }
+  return mcg_exp_ff_core(t, delta, T);
 }
 
 /* Below this argument 1 - expf(t) rounds to exactly 1.0f whatever expf

@@ -59,7 +59,7 @@ __device__ __forceinline__ void fit_ff_add(float &hi, float &lo, float v)
   lo = __fadd_rn(lo, e);
 }
 
-__global__ void __launch_bounds__(512) mcg_fit_kernel(mcg_fit_params P)
+__global__ void __launch_bounds__(512, 2) mcg_fit_kernel(mcg_fit_params P)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   long long *s_ctl = reinterpret_cast<long long *>(smem);

@@ -127,40 +127,59 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
   const float edge = neg ? c.z : c.w;
   float om;
   if (STRICT) {
-    /* d_edge, and the crossing's absorption, do not depend on the flight
-     * sample: start them before the logarithm */
+    /* The certain crossing, computed without branches: d_edge by the cached
+     * reciprocal, the crossing's absorption by the exp evaluator, and the
+     * certified bound.  It is the reference's step exactly when every
+     * condition in `easy` holds (division and exp arguments in the range
+     * where those forms are exact, no exception-table candidate, a flight
+     * certainly past the edge); almost every step of a fine mesh is such a
+     * crossing.  Any other step takes the full step below with the same h. */
     const float a = __fsub_rn(edge, x), aa = fabsf(a);
-    const float de = inv_mu == 0.0f ? MCG_MAXREAL
-                     : (aa >= 0x1p-100f && aa <= 0x1p100f) ? mcg_div_by_rcp(a, mu, inv_mu)
-                                                            : __fdiv_rn(a, mu);
-    const float om_cross = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, de), T, LM);
-    /* di = sig_i > EPS ? -log(h) / sig_i : MAXREAL; the exact value is
-     * only needed when the flight may end inside the cell: the certified
-     * test h < ~exp(-sig_i de) settles almost every crossing */
-    bool cross;
-    float di = MCG_MAXREAL;
-    if (c.y > MCG_EPS) {
-      const float bound = __fmul_rn(
-          mcg_ex2_approx(__fmul_rn(__fmul_rn(c.y, de), -MCG_LOG2E_F)), MCG_CROSS_FACTOR);
-      if (h < bound) {
-        cross = true;
+    const float de_q = mcg_div_by_rcp(a, mu, inv_mu);
+    const float t_q = __fmul_rn(-sig_a, de_q);
+    float d_q;
+    const float y_q = mcg_exp_ff_core(t_q, &d_q, T);
+    const float bound_q = __fmul_rn(
+        mcg_ex2_approx(__fmul_rn(__fmul_rn(c.y, de_q), -MCG_LOG2E_F)), MCG_CROSS_FACTOR);
+    const bool easy = (inv_mu != 0.0f) & (aa >= 0x1p-100f) & (aa <= 0x1p100f) &
+                      (t_q >= MCG_EXP_ONE_BOUND) & (t_q < 89.0f) & (d_q > LM.tau_exp_max) &
+                      (c.y > MCG_EPS) & (h < bound_q);
+    bool cross = true;
+    float de = de_q, di = MCG_MAXREAL;
+    if (easy) {
+      x = edge;
+      om = __fsub_rn(1.0f, y_q);
+    } else {
+      /* d_edge, and the crossing's absorption, do not depend on the flight
+       * sample: start them before the logarithm */
+      de = inv_mu == 0.0f ? MCG_MAXREAL
+           : (aa >= 0x1p-100f && aa <= 0x1p100f) ? de_q
+                                                  : __fdiv_rn(a, mu);
+      const float om_cross = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, de), T, LM);
+      /* di = sig_i > EPS ? -log(h) / sig_i : MAXREAL; the exact value is
+       * only needed when the flight may end inside the cell: the certified
+       * test h < ~exp(-sig_i de) settles almost every crossing */
+      if (c.y > MCG_EPS) {
+        const float bound = __fmul_rn(
+            mcg_ex2_approx(__fmul_rn(__fmul_rn(c.y, de), -MCG_LOG2E_F)), MCG_CROSS_FACTOR);
+        if (!(h < bound)) {
+          di = __fdiv_rn(-mcg_logf_strict(h, T, LM), c.y);
+          cross = !(di < de);
+        }
       } else {
-        di = __fdiv_rn(-mcg_logf_strict(h, T, LM), c.y);
         cross = !(di < de);
       }
-    } else {
-      cross = !(di < de);
-    }
-    if (!cross) {
-      inew = idx;
-      x = __fadd_rn(x, __fmul_rn(di, mu));
-      mu = __fsub_rn(__fmul_rn(2.0f, mcg_rnd_real(seed)), 1.0f);
-      inv_mu = mcg_flight_rcp(mu);
-      om = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, di), T, LM);
-      ++nsc;
-    } else {
-      x = edge;
-      om = om_cross;
+      if (!cross) {
+        inew = idx;
+        x = __fadd_rn(x, __fmul_rn(di, mu));
+        mu = __fsub_rn(__fmul_rn(2.0f, mcg_rnd_real(seed)), 1.0f);
+        inv_mu = mcg_flight_rcp(mu);
+        om = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, di), T, LM);
+        ++nsc;
+      } else {
+        x = edge;
+        om = om_cross;
+      }
     }
     const float dw = __fmul_rn(om, wmc);
     wmc = __fsub_rn(wmc, dw);
