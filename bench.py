@@ -276,6 +276,11 @@ def run_gpu(args):
     # roofline of the tracker kernel: algorithmic bytes per launch
     hbm_peak, peak_kind = peaks()
     bytes_per_hist = 24 + 24 + 4  # particle in, particle out, result
+    # DRAM bytes (read + write) per history of one ncu capture of this kernel
+    # (3e6 histories, 112.4 MB; profiles/track_strict_slab10k_ncu.md), scaled
+    # to the launch: below the algorithmic 52 B because part of the particle
+    # write-back is still in L2 when the kernel ends
+    dram_per_hist = 112.44e6 / 3e6
     mean_ms = sum(kernel_ms) / len(kernel_ms)
     achieved = bytes_per_hist * B / (mean_ms / 1e3) / 1e9
     steps_per_s = counters["steps"] / dev_s if not dist else None
@@ -302,7 +307,9 @@ def run_gpu(args):
         "e2e": {"value": e2e_val * ws, "unit": "histories/s",
                 "h2d_bytes_per_step": 24 * B, "d2h_bytes_per_step": 28 * B + 8 * NB_CELLS},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
+                     "frac": achieved / hbm_peak,
+                     "traffic": dram_per_hist * B if args.mode == "strict" else None,
+                     "traffic_unit": "bytes per launch (ncu capture of 3e6 histories, scaled)",
                      "peak_source": peak_kind,
                      "note": "the tracker is issue-bound; see issue_roofline"},
         "issue_roofline": {"bound": "issue", "n_alg_ops_per_step": n_alg,

@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
   unsigned long long *s_cnt = reinterpret_cast<unsigned long long *>(smem + sizeof(mcg_libm_tab));
   unsigned long long *s_tally = s_cnt + 16;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int ncell = P.n_cells, lo = P.cell_lo, hi = P.cell_lo + P.n_cells;
+  const int ncell = P.n_cells, lo = P.cell_lo;
 
   if (STRICT) {
     const float *src = reinterpret_cast<const float *>(P.libm_tab);
@@ -291,6 +291,7 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
       if (!active && my >= 0) {
         hid = my;
         mcg_load_particle(P, hid, seed, x, mu, wmc, idx);
+        idx -= lo;
         inv_mu = mcg_flight_rcp(mu);
         nst = nsc = 0;
         active = true;
@@ -299,17 +300,32 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
     if (!__any_sync(0xffffffffu, active))
       break;
 
-    for (int k = 0; k < P.refill_steps; ++k) {
-      if (!active)
-        break;
-      if (!((wmc >= min_w) && (idx < hi) && (idx >= lo)) || nst >= P.max_steps) {
-        /* history ends: classification of simulate_particle */
+    if (active) {
+      /* up to refill_steps steps, never past the step limit; idx is the
+       * cell index local to the chain, so one unsigned compare is the
+       * range test of simulate_particle's loop */
+      const int kmax = (int)min((uint32_t)P.refill_steps, P.max_steps - nst);
+      int k = 0;
+      bool going = true;
+      for (; k < kmax; ++k) {
+        if (!((wmc >= min_w) & ((unsigned)idx < (unsigned)ncell))) {
+          going = false;
+          break;
+        }
+        mcg_step<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + idx),
+                                &my_tally[idx], qs, T, P.libm);
+      }
+      nst += (uint32_t)k;
+      if (!going || nst >= P.max_steps) {
+        /* history ends: classification of simulate_particle; a history
+         * still alive in the chain here has reached the step limit */
+        const bool in = (wmc >= min_w) && ((unsigned)idx < (unsigned)ncell);
         int r;
-        if (nst >= P.max_steps && (wmc >= min_w) && (idx < hi) && (idx >= lo))
+        if (in)
           r = 2;
-        else if (idx == lo - 1)
+        else if (idx == -1)
           r = -1;
-        else if (idx == hi)
+        else if (idx == ncell)
           r = 1;
         else if (wmc < min_w)
           r = 0;
@@ -321,7 +337,7 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
           q[1] = (unsigned long long)__float_as_uint(x) |
                  ((unsigned long long)__float_as_uint(mu) << 32);
           q[2] = (unsigned long long)__float_as_uint(wmc) |
-                 ((unsigned long long)(uint32_t)idx << 32);
+                 ((unsigned long long)(uint32_t)(idx + lo) << 32);
         }
         if (P.results)
           P.results[hid] = r;
@@ -346,11 +362,7 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
         tot_steps += nst;
         tot_scat += nsc;
         active = false;
-        break;
       }
-      mcg_step<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + (idx - lo)),
-                              &my_tally[idx - lo], qs, T, P.libm);
-      ++nst;
     }
   }
 

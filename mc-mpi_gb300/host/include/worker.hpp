@@ -12,8 +12,12 @@
  * async and rma strategies of the reference differ only in how the MPI
  * messages travel; on one GPU they are the same queues, so WorkerSync,
  * WorkerAsync and WorkerRma name this class.  dump() writes out/config.yaml,
- * out/weights.csv and WA.out in the reference's formats
- * (src/worker.cpp:36-61, 218-241, 287-313; src/layer.cpp:363-380).
+ * out/weights.csv, out/stats.csv and WA.out in the reference's formats
+ * (src/worker.cpp:36-61, 63-181, 218-241, 287-313; src/layer.cpp:363-380).
+ * stats.csv has WorkerSync's columns (the timer's, no message counts: the
+ * hand-over is part of the GPU cycle, so its send, receive and idle times
+ * are zero and the computation time is the GPU time of spin()), one row per
+ * sub-domain.
  */
 #ifndef MCG_WORKER_HPP
 #define MCG_WORKER_HPP
@@ -56,6 +60,7 @@ public:
   const MCMPIOptions options;
   long long cycles = 0, handoffs = 0; /* of the last spin() */
   float seconds = 0.f;                /* GPU time of the last spin() */
+  double starttime = 0.0, endtime = 0.0; /* wall clock (CLOCK_REALTIME) around spin() */
 
 private:
   mcg_context *ctx_ = nullptr;

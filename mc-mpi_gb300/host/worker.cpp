@@ -8,12 +8,22 @@
 #include <fstream>
 #include <map>
 #include <sys/stat.h>
+#include <time.h>
 #include <unistd.h>
 
 static void die(const char *what)
 {
   fprintf(stderr, "%s: %s\n", what, mcg_last_error());
   exit(EXIT_FAILURE);
+}
+
+/* Wall clock in seconds, the time base of the reference's timer stamps
+ * (MPI_Wtime shifted to CLOCK_REALTIME, src/timer.cpp:7-24). */
+static double wall_seconds()
+{
+  struct timespec t;
+  clock_gettime(CLOCK_REALTIME, &t);
+  return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
 }
 
 MCMPIOptions options_from_config(std::string filepath, int world_size)
@@ -102,10 +112,12 @@ void Worker::spin()
                     (int32_t)(options.x_ini / dx_[src_layer])};
   int64_t cyc = 0, hand = 0;
   const int64_t cap = (int64_t)options.nb_particles + 1;
+  starttime = wall_seconds();
   if (mcg_worker_run(ctx_, &src, (int64_t)options.nb_particles,
                      options.nb_particles_per_cycle > 0 ? options.nb_particles_per_cycle : 65536,
                      cap, &cyc, &hand) != MCG_OK)
     die("Worker::spin");
+  endtime = wall_seconds();
   cycles = cyc;
   handoffs = hand;
   mcg_last_kernel_ms(ctx_, &seconds);
@@ -160,6 +172,17 @@ void Worker::dump()
       proc++;
     fprintf(f, "%d, %.18e, %.18e\n", proc, dx_[0] * (i + 0.5), w[i] / dx_[0]);
   }
+  fclose(f);
+  /* out/stats.csv (src/worker.cpp:63-181) with WorkerSync's columns: one
+   * timer state per sub-domain (the whole spin), no message counts */
+  f = fopen((foldername + "/stats.csv").c_str(), "w");
+  if (!f)
+    die("Worker::dump");
+  fprintf(f, "rank, starttime, endtime, time_comp, time_send, time_recv, time_idle, "
+             "nb_cycles, \n");
+  for (int r = 0; r < options.world_size; ++r)
+    fprintf(f, "%d, %.18e, %.18e, %.18e, %.18e, %.18e, %.18e, %d, \n", r, starttime, endtime,
+            (double)seconds, 0.0, 0.0, 0.0, (int)cycles);
   fclose(f);
   /* WA.out of rank 0's layer (Layer::dump_WA) */
   f = fopen("WA.out", "w");

@@ -51,6 +51,15 @@ def test_cpp_worker_outputs(built, mcg, tmp_path):
     assert procs[0] == 0 and procs[-1] == 7 and procs == sorted(procs)
     assert (tmp_path / "out" / "config.yaml").read_text().startswith("# Read from config")
     assert len((tmp_path / "WA.out").read_text().splitlines()) == 125
+    # out/stats.csv in WorkerSync's columns, one row per sub-domain
+    stats = (tmp_path / "out" / "stats.csv").read_text().splitlines()
+    assert stats[0] == ("rank, starttime, endtime, time_comp, time_send, time_recv, "
+                        "time_idle, nb_cycles, ")
+    assert len(stats) == 9
+    for r, row in enumerate(stats[1:]):
+        f = [x.strip() for x in row.split(",")]
+        assert int(f[0]) == r and len(f) == 9 and f[8] == ""
+        assert float(f[2]) >= float(f[1]) > 0 and float(f[3]) > 0 and int(f[7]) > 0
     # the same problem through the fused tracker: identical absorbed weights
     w = np.array([float(x.split(",")[2]) for x in rows[1:]])
     st, m, dx, _, _ = mcg.layer_decomposition(0.0, 1.0, 1000, 8)
