@@ -147,12 +147,26 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
       }
       if (!__any_sync(0xffffffffu, active))
         break;
-      for (int k = 0; k < P.refill_steps; ++k) {
-        if (!active)
-          break;
-        if (!((wmc >= min_w) && (idx < m) && (idx >= 0)) || nst >= P.max_steps) {
+      if (active) {
+        /* up to refill_steps steps, never past the step limit; one
+         * unsigned compare is the slab's range test */
+        const int kmax = (int)min((uint32_t)P.refill_steps, P.max_steps - nst);
+        int k = 0;
+        bool going = true;
+        for (; k < kmax; ++k) {
+          if (!((wmc >= min_w) & ((unsigned)idx < (unsigned)m))) {
+            going = false;
+            break;
+          }
+          mcg_step<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(cells + idx),
+                                  &tally[idx], qs, T, P.libm);
+        }
+        nst += (uint32_t)k;
+        if (!going || nst >= P.max_steps) {
+          /* a history still alive in the slab here has reached the limit */
+          const bool in = (wmc >= min_w) && ((unsigned)idx < (unsigned)m);
           int r;
-          if (nst >= P.max_steps && (wmc >= min_w) && (idx < m) && (idx >= 0))
+          if (in)
             r = 2;
           else if (idx == -1)
             r = -1;
@@ -179,11 +193,7 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
           tot_steps += nst;
           tot_scat += nsc;
           active = false;
-          break;
         }
-        mcg_step<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(cells + idx),
-                                &tally[idx], qs, T, P.libm);
-        ++nst;
       }
     }
   }
