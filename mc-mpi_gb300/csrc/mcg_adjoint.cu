@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(1024) mcg_adjoint_kernel(mcg_adj_params P)
   float *s_ga = reinterpret_cast<float *>(s_tally + P.n_cells);
   float *s_gs = s_ga + P.n_cells;
   const int tid = threadIdx.x, lane = tid & 31;
-  const int ncell = P.n_cells, lo = P.cell_lo, hi = P.cell_lo + P.n_cells;
+  const int ncell = P.n_cells, lo = P.cell_lo;
   if (STRICT) {
     const float *src = reinterpret_cast<const float *>(P.libm_tab);
     float *dst = reinterpret_cast<float *>(T);
@@ -125,6 +125,7 @@ __global__ void __launch_bounds__(1024) mcg_adjoint_kernel(mcg_adj_params P)
       if (!active && my >= 0) {
         hid = my;
         mcg_source_particle(P.src, P.first + hid, seed, x, mu, wmc, idx);
+        idx -= lo;
         inv_mu = mcg_flight_rcp(mu);
         nst = nsc = 0;
         phase = 0;
@@ -135,54 +136,61 @@ __global__ void __launch_bounds__(1024) mcg_adjoint_kernel(mcg_adj_params P)
     if (!__any_sync(0xffffffffu, active))
       break;
 
-    for (int k = 0; k < P.refill_steps; ++k) {
-      if (!active)
-        break;
-      if (!((wmc >= min_w) && (idx < hi) && (idx >= lo)) || nst >= P.max_steps) {
-        if (nst >= P.max_steps && (wmc >= min_w) && (idx < hi) && (idx >= lo))
-          atomicOr(&s_cnt[MCG_CNT_ERR], 1ull);
-        if (phase == 0 && P.with_grad) {
-          /* replay the same history from its start */
-          tot_steps += nst;
-          tot_scat += nsc;
-          mcg_source_particle(P.src, P.first + hid, seed, x, mu, wmc, idx);
-          inv_mu = mcg_flight_rcp(mu);
-          nst = nsc = 0;
-          phase = 1;
-          continue;
+    if (active) {
+      /* up to refill_steps steps, never past the step limit; idx is local
+       * to the chain */
+      const int kmax = (int)min((uint32_t)P.refill_steps, P.max_steps - nst);
+      int k = 0;
+      bool going = true;
+      for (; k < kmax; ++k) {
+        if (!((wmc >= min_w) & ((unsigned)idx < (unsigned)ncell))) {
+          going = false;
+          break;
         }
+        const int c = idx;
+        const float2 ax = __ldg(P.aux + c);
+        float l, dep;
+        bool coll;
+        mcg_step<STRICT, MCG_TALLY_SMEM32>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + c),
+                                           phase == 0 ? &s_tally[c] : nullptr, qs, T, P.libm, &l,
+                                           &coll, &dep);
+        const float g = __fmul_rn(ax.x, dep);
+        if (phase == 0) {
+          ff_add(G_hi, G_lo, g);
+        } else {
+          /* suffix before this step, then after it */
+          const float v_before = __fadd_rn(__fsub_rn(G_hi, P_hi), __fsub_rn(G_lo, P_lo));
+          ff_add(P_hi, P_lo, g);
+          const float v_after = __fadd_rn(__fsub_rn(G_hi, P_hi), __fsub_rn(G_lo, P_lo));
+          const float ga = l * (ax.x * wmc - v_after);
+          const float score = (coll ? ax.y : 0.0f) - l;
+          const float gsc = score * v_before;
+          atomicAdd(&s_ga[c], ga);
+          atomicAdd(&s_gs[c], gsc);
+        }
+      }
+      nst += (uint32_t)k;
+      if (!going || nst >= P.max_steps) {
+        if ((wmc >= min_w) && ((unsigned)idx < (unsigned)ncell))
+          atomicOr(&s_cnt[MCG_CNT_ERR], 1ull); /* the step limit */
         if (phase == 0) {
           tot_steps += nst;
           tot_scat += nsc;
         }
-        atomicAdd(&s_cnt[MCG_CNT_HIST], 1ull);
-        mcg_tally_add<MCG_TALLY_SMEM32>(&s_cnt[MCG_CNT_WLEFT],
-                                         mcg_to_fixed(G_hi, gs) + mcg_to_fixed(G_lo, gs));
-        active = false;
-        break;
+        if (phase == 0 && P.with_grad) {
+          /* replay the same history from its start */
+          mcg_source_particle(P.src, P.first + hid, seed, x, mu, wmc, idx);
+          idx -= lo;
+          inv_mu = mcg_flight_rcp(mu);
+          nst = nsc = 0;
+          phase = 1;
+        } else {
+          atomicAdd(&s_cnt[MCG_CNT_HIST], 1ull);
+          mcg_tally_add<MCG_TALLY_SMEM32>(&s_cnt[MCG_CNT_WLEFT],
+                                           mcg_to_fixed(G_hi, gs) + mcg_to_fixed(G_lo, gs));
+          active = false;
+        }
       }
-      const int c = idx - lo;
-      const float2 ax = __ldg(P.aux + c);
-      float l, dep;
-      bool coll;
-      mcg_step<STRICT, MCG_TALLY_SMEM32>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + c),
-                                         phase == 0 ? &s_tally[c] : nullptr, qs, T, P.libm, &l,
-                                         &coll, &dep);
-      const float g = __fmul_rn(ax.x, dep);
-      if (phase == 0) {
-        ff_add(G_hi, G_lo, g);
-      } else {
-        /* suffix before this step, then after it */
-        const float v_before = __fadd_rn(__fsub_rn(G_hi, P_hi), __fsub_rn(G_lo, P_lo));
-        ff_add(P_hi, P_lo, g);
-        const float v_after = __fadd_rn(__fsub_rn(G_hi, P_hi), __fsub_rn(G_lo, P_lo));
-        const float ga = l * (ax.x * wmc - v_after);
-        const float score = (coll ? ax.y : 0.0f) - l;
-        const float gsc = score * v_before;
-        atomicAdd(&s_ga[c], ga);
-        atomicAdd(&s_gs[c], gsc);
-      }
-      ++nst;
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
