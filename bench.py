@@ -19,8 +19,9 @@ value : histories/s of the strict tracker with the batch's particles
         already resident in HBM (mcg_simulate_device), CUDA-event time of
         the kernel, L2 flushed (256 MB memset) between steps.
 e2e   : histories/s through the C ABI with host buffers (mcg_simulate on
-        pinned host particles: H2D particles, kernel, D2H particles +
-        results + tally), wall time per step.
+        pinned host particles and results, which the tracker reads and
+        writes in place over the host link, + the tally read), wall time per
+        step.
 --impl reference : the reference's CPU implementation of the path (the
         oracle port of src/layer.cpp on all host cores), same metric.
 """
@@ -305,7 +306,9 @@ def run_gpu(args):
         "wall_s": wall,
         "gpu_launches": args.steps,
         "e2e": {"value": e2e_val * ws, "unit": "histories/s",
-                "h2d_bytes_per_step": 24 * B, "d2h_bytes_per_step": 28 * B + 8 * NB_CELLS},
+                "h2d_bytes_per_step": 24 * B, "d2h_bytes_per_step": 28 * B + 8 * NB_CELLS,
+                "path": "mcg_simulate on pinned host buffers: the tracker reads and writes "
+                        "them in place over the host link during the launch"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak,
                      "traffic": dram_per_hist * B if args.mode == "strict" else None,

@@ -101,7 +101,10 @@ int mcg_tally_read(mcg_context *ctx, int64_t *h_q, double *h_f64);
 /* Run histories of n host particles (Particle array, updated in place with
  * the final state).  h_results (may be NULL): -1/0/+1 per particle.
  * h_steps, h_scatters (may be NULL): particle_step calls and in-cell
- * scatters per particle.  Host<->device copies included. */
+ * scatters per particle.  When every given buffer is page-locked (pinned or
+ * registered host memory), the GPU reads and writes them in place (each
+ * particle crosses the host link once each way during the launch);
+ * otherwise they are copied through device memory.  Synchronous. */
 int mcg_simulate(mcg_context *ctx, mcg_particle *h_particles, int64_t n, int32_t *h_results,
                  int64_t *h_steps, int64_t *h_scatters);
 

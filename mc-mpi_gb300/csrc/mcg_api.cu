@@ -628,6 +628,22 @@ static int ensure_scratch(mcg_context *ctx, int64_t n)
   return MCG_OK;
 }
 
+/* Device address of a page-locked (pinned or registered) host buffer, or
+ * nullptr for pageable memory.  Pinned memory is mapped into the device's
+ * address space (unified addressing), so the tracker can read and write it
+ * in place: over NVLink-C2C on Grace machines, over PCIe elsewhere. */
+static void *pinned_device_ptr(const void *h)
+{
+  if (!h)
+    return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError(); /* clear the (non-sticky) error of an unknown pointer */
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 extern "C" int mcg_simulate(mcg_context *ctx, mcg_particle *h_particles, int64_t n,
                             int32_t *h_results, int64_t *h_steps, int64_t *h_scatters)
 {
@@ -636,8 +652,20 @@ extern "C" int mcg_simulate(mcg_context *ctx, mcg_particle *h_particles, int64_t
   if (n == 0)
     return MCG_OK;
   int rc = ensure_device(ctx);
-  if (rc == MCG_OK)
-    rc = ensure_scratch(ctx, n);
+  if (rc != MCG_OK)
+    return rc;
+  /* every buffer page-locked: one history reads and writes its 24-byte
+   * particle once over ~1e2-1e4 steps, so the tracker works on the host
+   * buffers in place instead of copying them through device memory */
+  void *zp = pinned_device_ptr(h_particles);
+  void *zr = pinned_device_ptr(h_results), *zs = pinned_device_ptr(h_steps);
+  void *zc = pinned_device_ptr(h_scatters);
+  if (zp && (!h_results || zr) && (!h_steps || zs) && (!h_scatters || zc)) {
+    rc = mcg_track_launch(ctx, static_cast<mcg_particle *>(zp), n, static_cast<int32_t *>(zr),
+                          static_cast<int64_t *>(zs), static_cast<int64_t *>(zc), nullptr, 0);
+    return rc == MCG_OK ? mcg_sync(ctx) : rc;
+  }
+  rc = ensure_scratch(ctx, n);
   if (rc != MCG_OK)
     return rc;
   cudaError_t e = cudaMemcpyAsync(ctx->d_part, h_particles, n * sizeof(mcg_particle),

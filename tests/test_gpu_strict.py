@@ -149,6 +149,41 @@ def test_layer_api_simulate_batches(mcg, oracle):
     assert np.allclose(layer.weights_absorbed, ref["tally_f32"], rtol=1e-5, atol=1e-6)
 
 
+def test_simulate_pinned_buffers_in_place(ctx, mcg, oracle):
+    """mcg_simulate on page-locked host buffers (read and written in place by
+    the GPU) equals the staged path on pageable copies of the same
+    particles, byte for byte, results, steps and tallies included."""
+    import ctypes as C
+    import torch
+    nb, P, N = 10000, 64, 20000
+    st, m, dx, _, _ = mcg.layer_decomposition(0.0, 1.0, nb, P)
+    xc = (np.arange(nb) + 0.5) / nb
+    sa = (0.5 + 0.4 * np.sin(6 * np.pi * xc)).astype(np.float32)
+    ss = (2.0 + 1.5 * np.cos(4 * np.pi * xc)).astype(np.float32)
+    sigs = (sa + ss).astype(np.float32)
+    ctx.set_layers(st, m, dx, sigs, (sa / sigs).astype(np.float32), 1e-12)
+    p = np.zeros(N, mcg.PARTICLE_DTYPE)
+    p["seed"] = oracle.rnd_seed_chain(77, N)
+    p["mu"], p["wmc"] = 1.0, 1.0
+    staged = p.copy()
+    ctx.tally_reset()
+    r0 = ctx.simulate(staged)
+    q0 = ctx.tally_q()
+    hp = torch.from_numpy(p.view(np.uint8).copy()).pin_memory()
+    hr = torch.full((N,), 9, dtype=torch.int32).pin_memory()
+    hs = torch.zeros(N, dtype=torch.int64).pin_memory()
+    hc = torch.zeros(N, dtype=torch.int64).pin_memory()
+    ctx.tally_reset()
+    rc = ctx.lib.mcg_simulate(ctx.h, C.c_void_p(hp.data_ptr()), N, C.c_void_p(hr.data_ptr()),
+                              C.c_void_p(hs.data_ptr()), C.c_void_p(hc.data_ptr()))
+    assert rc == 0, ctx.lib.mcg_last_error().decode()
+    assert hp.numpy().tobytes() == staged.tobytes()
+    assert np.array_equal(hr.numpy(), r0["results"])
+    assert np.array_equal(hs.numpy(), r0["steps"])
+    assert np.array_equal(hc.numpy(), r0["scatters"])
+    assert np.array_equal(ctx.tally_q(), q0)
+
+
 def test_rnd_real_device_kat(ctx, oracle):
     """src/test_curandom.cu: device rnd_real == CPU, seeds and floats."""
     import torch
