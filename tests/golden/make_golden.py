@@ -14,7 +14,9 @@ Fixtures:
                       particle as the reference lays it out.
   traces_*.npz        per-particle histories through the reference's public
                       Layer::particle_step with simulate_particle's loop:
-                      initial and final particles, result, steps, scatters.
+                      initial and final particles, result, steps, scatters
+                      (traces_edge: the step's special cases, see
+                      edge_case_physics and edge_case_particles).
   decomposed_*.npz    reference float tallies of a decomposed slab driven by
                       the WorkerSync cycle over Layer::simulate.
 """
@@ -74,6 +76,52 @@ def ref_traces(name, L, sigs, rates, min_w, particles):
     print(f"traces_{name}: n={len(fin)} mean steps {tr['steps'].mean():.1f}")
 
 
+def edge_case_physics(m):
+    """Cells cycling through the step's special cases: vacuum (sigs = 0),
+    pure absorber (rate 1, sig_i = 0), sig_i on the EPS threshold
+    (2e-4 * 0.5), optically thick scatterer and absorber (exp arguments
+    below -17.5), and an ordinary cell."""
+    kinds = [(0.0, 0.5), (3.0, 1.0), (2e-4, 0.5), (5000.0, 0.3), (2000.0, 0.99), (2.5, 0.2)]
+    sigs = np.array([kinds[i % 6][0] for i in range(m)], np.float32)
+    rates = np.array([kinds[i % 6][1] for i in range(m)], np.float32)
+    return sigs, rates
+
+
+def edge_case_particles(L, n, base=424242):
+    """Particles mixing ordinary starts with the special ones: directions 0,
+    -0, +-1e-4 (the EPS threshold), 1e-5, +-1; positions exactly on cell
+    edges (either neighbouring index) and one ulp past them; indices just
+    outside the layer; weights at, below and far below the minimum."""
+    rng = np.random.default_rng(7)
+    p = chain_particles(n, 0.0, 1.0, 1.0, L.index_start, base)
+    cells = rng.integers(L.index_start, L.index_start + L.m, n)
+    frac = rng.random(n).astype(np.float32)
+    x = ((cells.astype(np.float32) + frac) * f32(L.dx)).astype(np.float32)
+    idx = cells.astype(np.int32)
+    mu = rng.uniform(-1.0, 1.0, n).astype(np.float32)
+    w = np.ones(n, np.float32)
+    special_mu = np.array([0.0, -0.0, 1e-4, -1e-4, 1.0001e-4, 1e-5, 1.0, -1.0], np.float32)
+    k = rng.integers(0, 10, n)
+    pick = k < 3
+    mu[pick] = special_mu[rng.integers(0, len(special_mu), pick.sum())]
+    edge = k == 3                        # on the left edge of the cell
+    x[edge] = (cells[edge].astype(np.float32) * f32(L.dx)).astype(np.float32)
+    edge_r = k == 4                      # on the same edge, owned by the cell before
+    x[edge_r] = (cells[edge_r].astype(np.float32) * f32(L.dx)).astype(np.float32)
+    idx[edge_r] = np.maximum(cells[edge_r] - 1, L.index_start)
+    past = k == 5                        # one ulp past the left edge, inwards and out
+    e = (cells[past].astype(np.float32) * f32(L.dx)).astype(np.float32)
+    x[past] = np.where(rng.random(past.sum()) < 0.5, np.nextafter(e, f32(-1)),
+                       np.nextafter(e, f32(2))).astype(np.float32)
+    low = k == 6
+    w[low] = np.array([1e-12, 9e-13, 0.0, 1.5e-12], np.float32)[rng.integers(0, 4, low.sum())]
+    out = k == 7
+    idx[out] = np.array([L.index_start - 1, L.index_start + L.m, L.index_start - 5],
+                        np.int32)[rng.integers(0, 3, out.sum())]
+    p["x"], p["mu"], p["wmc"], p["index"] = x, mu, w, idx
+    return p
+
+
 def main():
     if not O.ref_available():
         O.build()
@@ -122,6 +170,12 @@ def main():
     sigs, rates = sigs_rates(sa, ss)
     ps = chain_particles(2000, float(f32(L.index_start) * L.dx), 1.0, 1.0, L.index_start)
     ref_traces("sublayer", L, sigs, rates, 1e-12, ps)
+
+    # 4d. edge cases of particle_step / simulate_particle on a middle
+    # sub-domain (cells 60..119 of 240 in 4 layers)
+    L = O.decompose(0.0, 1.0, 240, 4)[1]
+    sigs, rates = edge_case_physics(L.m)
+    ref_traces("edge", L, sigs, rates, 1e-12, edge_case_particles(L, 4000))
 
     # 5. decomposed slab: reference float tallies (WorkerSync cycle)
     nb, P, N = 1000, 8, 4000

@@ -64,7 +64,7 @@ def test_particle_layout(mcg):
     assert fnv1a_signed_char(p.tobytes()) == int(load("particle_hash.npz")["hash"])
 
 
-@pytest.mark.parametrize("name", ["config0", "default1000", "sublayer"])
+@pytest.mark.parametrize("name", ["config0", "default1000", "sublayer", "edge"])
 def test_oracle_matches_reference_traces(oracle, name):
     """Per particle, bit for bit: final state, result, steps, scatters."""
     g = load(f"traces_{name}.npz")
