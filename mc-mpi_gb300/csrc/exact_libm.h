@@ -173,11 +173,11 @@ MCG_HD float mcg_exp_ff_core(float t, float *delta, const mcg_libm_tab *T)
     float lo = MCG_ADD(se, r2);
     float yh = MCG_ADD(s, lo);
     float yl = MCG_ADD(MCG_SUB(s, yh), lo);
-    /* mcg_midpoint_delta for yh in [0.99, 1.01]: the spacing on yl's side is
-     * 2^-24 below 1 (and below 1.0 itself), 2^-23 from 1 up */
-    const uint32_t ub = mcg_f2u(yh);
-    const bool below = ub < 0x3f800000u || (ub == 0x3f800000u && yl < 0.0f);
-    *delta = MCG_SUB(0.5f, MCG_MUL(fabsf(yl), below ? 16777216.0f : 8388608.0f));
+    /* distance from the rounding midpoint in units of 2^-24, the float
+     * spacing below 1 (every t < 0); above 1 the spacing is 2^-23 and this
+     * measure is only a filter key, which the table generator, running this
+     * same code, sets its thresholds by */
+    *delta = MCG_SUB(0.5f, MCG_MUL(fabsf(yl), 16777216.0f));
     return yh;
   }
   float kf = mcg_int_to_float(k);

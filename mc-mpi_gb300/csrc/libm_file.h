@@ -49,7 +49,7 @@ static inline uint64_t mcg_fnv_word(uint64_t h, float v)
 
 /* FNV-1a over the bits of logf/expf and of the evaluators at 8192
  * arguments spread over both domains by a 32-bit LCG (the exp arguments
- * cover both evaluator paths). */
+ * cover both evaluator paths and both signs). */
 static inline uint64_t mcg_libm_fingerprint(const mcg_libm_tab *T)
 {
   uint64_t h = 1469598103934665603ull;
@@ -60,7 +60,7 @@ static inline uint64_t mcg_libm_fingerprint(const mcg_libm_tab *T)
     float x, d, t = 0.0f;
     memcpy(&x, &ux, 4);
     if (i & 1)
-      t = (i & 2) ? -x * 17.0f : -x * 0.005f;
+      t = (i & 2) ? -x * 17.0f : (i & 4) ? x * 0.005f : -x * 0.005f;
     h = mcg_fnv_word(h, (i & 1) ? expf(t) : logf(x));
     h = mcg_fnv_word(h, (i & 1) ? mcg_exp_ff(t, &d, T) : mcg_log_ff(x, &d, T));
     h = mcg_fnv_word(h, d);
