@@ -46,6 +46,9 @@ METRIC = "histories/s on 1 GB300 (plain vs batched vs fwd+adjoint) at matched ta
 NB_CELLS, N_LAYERS, N_TOTAL = 10000, 64, 100_000_000
 BASE_SEED = 5127801
 MIN_W = 1e-12
+WORKLOAD = ("slab 10000 cells / 64 sub-domains (decompose_domain), sigma_a=0.5+0.4sin(6pi x), "
+            "sigma_s=2+1.5cos(4pi x), 1e8 histories from x=0 mu=1 w=1, rnd_seed chain 5127801, "
+            "min weight 1e-12")
 
 
 def peaks():
@@ -171,7 +174,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": "slab 10000 cells / 64 sub-domains, 1e8 histories from x=0 mu=1",
+        "config": {"workload": WORKLOAD,
                    "batch": per_step, "l2": "n/a (host)"},
         "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port",
                          "sample": f"{per_step} histories per step"},
@@ -296,9 +299,7 @@ def run_gpu(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "slab 10000 cells / 64 sub-domains (decompose_domain), sigma_a="
-                               "0.5+0.4sin(6pi x), sigma_s=2+1.5cos(4pi x), 1e8 histories from "
-                               "x=0 mu=1 w=1, rnd_seed chain 5127801, min weight 1e-12",
+        "config": {"workload": WORKLOAD,
                    "batch": B, "mode": args.mode, "parallelism": f"histories sharded x{ws}",
                    "l2": "flushed between steps (256 MB memset)"},
         "steps_per_s": counters["steps"] / dev_s * ws,
