@@ -202,8 +202,10 @@ int mcg_cusimulate(int n, mcg_particle *particles, const float *sigs, const floa
  * reference's bounded buffers); the n particles of the source are fed to the
  * sub-domain holding src->cell0; the loop ends when all n histories are
  * finished.  Tallies and counters as the other entry points; *h_cycles and
- * *h_handoffs (may be NULL) report the cycles run and the particles handed
- * over between sub-domains. */
+ * *h_handoffs (may be NULL) report the cycles that had particles to simulate
+ * and the particles handed over between sub-domains.  Each cycle's particles
+ * of all sub-domains are spread over the whole GPU, so a busy sub-domain is
+ * not limited to a fixed share of it. */
 int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n, int32_t per_cycle,
                    int64_t queue_capacity, int64_t *h_cycles, int64_t *h_handoffs);
 
