@@ -208,6 +208,7 @@ def run_gpu(args):
     ctx = mcg.Context(mode=args.mode, device=local)
     ctx.set_layers(st, m, dx, sigs, rates, MIN_W)
     ctx.set_tally_scale(35)
+    ctx.set_algorithm(args.algorithm, args.event_steps)
 
     # device-resident particles of the batch: built on the device by the
     # source kernel before the timed region (histories k*B .. of this rank)
@@ -265,7 +266,7 @@ def run_gpu(args):
     # e2e through the C ABI with pinned host buffers
     lib = mcg.load_library()
     e2e_times = []
-    for k in range(max(1, min(args.steps, 3)) + 1):
+    for k in range(0 if args.no_e2e else max(1, min(args.steps, 3)) + 1):
         make_batch(args.warmup + k)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
@@ -274,8 +275,7 @@ def run_gpu(args):
         tq = ctx.tally_q()
         e2e_times.append(time.perf_counter() - t1)
         built[0] = None  # the call wrote the final particle states back
-    e2e_s = statistics.median(e2e_times[1:])
-    e2e_val = B / e2e_s
+    e2e_val = B / statistics.median(e2e_times[1:]) if e2e_times else None
 
     # roofline of the tracker kernel: algorithmic bytes per launch
     hbm_peak, peak_kind = peaks()
@@ -300,16 +300,18 @@ def run_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": WORKLOAD,
-                   "batch": B, "mode": args.mode, "parallelism": f"histories sharded x{ws}",
+                   "batch": B, "mode": args.mode, "algorithm": args.algorithm,
+                   "parallelism": f"histories sharded x{ws}",
                    "l2": "flushed between steps (256 MB memset)"},
         "steps_per_s": counters["steps"] / dev_s * ws,
         "collisions_per_s": counters["scatters"] / dev_s * ws,
         "wall_s": wall,
         "gpu_launches": args.steps,
-        "e2e": {"value": e2e_val * ws, "unit": "histories/s",
-                "h2d_bytes_per_step": 24 * B, "d2h_bytes_per_step": 28 * B + 8 * NB_CELLS,
-                "path": "mcg_simulate on pinned host buffers: the tracker reads and writes "
-                        "them in place over the host link during the launch"},
+        "e2e": None if e2e_val is None else {
+            "value": e2e_val * ws, "unit": "histories/s",
+            "h2d_bytes_per_step": 24 * B, "d2h_bytes_per_step": 28 * B + 8 * NB_CELLS,
+            "path": "mcg_simulate on pinned host buffers: the tracker reads and writes "
+                    "them in place over the host link during the launch"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak,
                      "traffic": dram_per_hist * B if args.mode == "strict" else None,
@@ -321,6 +323,8 @@ def run_gpu(args):
                            "peak_gops": sms * 128 * f_sm / 1e9, "frac": issue_frac},
         "clocks": clocks,
     }
+    if rank == 0 and not args.no_extra and args.algorithm == "history":
+        line["event"] = bench_event(mcg, args.mode, local, st, m, dx, sigs, rates)
     if rank == 0 and not args.no_extra and args.mode == "strict":
         # the same steps with fast arithmetic (hardware log2/exp2; tallies
         # statistically equivalent, not bit-identical)
@@ -382,6 +386,31 @@ def bench_batched(mcg, mode, device, scale=0.02, reps=2):
             "steps_per_s": steps / t, "histories": n, "launches": 1,
             "workload": f"4096 slabs, cells U{{16..4096}}, L~U[0.5,5], sigma_a~U[0.1,5], "
                         f"sigma_s~U[0,10], histories log-uniform [1e3,1e6] x {scale}"}
+
+
+def bench_event(mcg, mode, device, st, m, dx, sigs, rates, n=10_000_000, k=4):
+    """The event-based tracker (SoA particle bank, K events per pass, per
+    event type compaction) on the first n histories of the workload, against
+    the history-based tracker on the same histories (identical tallies)."""
+    with mcg.Context(mode=mode, device=device) as ctx:
+        ctx.set_layers(st, m, dx, sigs, rates, MIN_W)
+        ctx.set_tally_scale(35)
+        ctx.simulate_source(0, n // 10)  # warm-up
+        ctx.tally_reset()
+        ctx.simulate_source(0, n)
+        t_hist = ctx.last_kernel_ms() / 1e3
+        q_hist = ctx.tally_q()
+        steps = ctx.counters()["steps"]
+        ctx.set_algorithm("event", k)
+        ctx.simulate_source(0, n // 10)  # sizes the bank
+        ctx.tally_reset()
+        ctx.simulate_source(0, n)
+        t_ev = ctx.last_kernel_ms() / 1e3
+        same = bool(np.array_equal(ctx.tally_q(), q_hist))
+    return {"value": n / t_ev, "unit": "histories/s", "steps_per_s": steps / t_ev,
+            "events_per_pass": k, "histories": n, "history_value": n / t_hist,
+            "identical_tallies": same,
+            "bank_bytes_per_event": 72 / k, "bank_gbs": 72 / k * steps / t_ev / 1e9}
 
 
 def bench_adjoint(mcg, mode, device, n=10_000_000):
@@ -505,6 +534,11 @@ def main():
     ap.add_argument("--mode", default="strict", choices=["strict", "fast"])
     ap.add_argument("--batch", type=int, default=N_TOTAL)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true",
+                    help="skip the e2e measurement (profiling runs)")
+    ap.add_argument("--algorithm", default="history", choices=["history", "event"],
+                    help="single-chain tracker: history-based (default) or event-based")
+    ap.add_argument("--event-steps", type=int, default=4, help="event mode: events per pass")
     ap.add_argument("--workload", default="plain", choices=["plain", "batch", "adjoint", "fit"])
     ap.add_argument("--scale", type=float, default=1.0,
                     help="fraction of the configuration's histories (batch, fit)")

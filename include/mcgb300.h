@@ -243,17 +243,26 @@ int mcg_batch_tally_read(mcg_context *ctx, int64_t *h_q, double *h_f64);
  * (as mcg_set_tally_mode). 0 keeps the current value. */
 int mcg_batch_set_launch(mcg_context *ctx, int32_t block, int64_t item_histories,
                          int32_t tally_mode);
-/* Autotuner: times every candidate launch shape on a sample of each slab's
- * histories (fraction in (0, 1]) and keeps the fastest.  Reports the choice
- * and its sample time; the batch tally and counters are reset afterwards. */
+/* Autotuner: times every candidate on a sample of each slab's histories
+ * (fraction in (0, 1]): the history-based launch shapes (block, histories
+ * per work item, tally privatisation) and the event-based form at 4 and 16
+ * events per pass, and keeps the fastest.  Reports the choice and its sample
+ * time; the batch tally and counters are reset afterwards. */
 typedef struct mcg_batch_tuning {
   int32_t block;
   int32_t tally_mode;
   int64_t item_histories;
   float sample_ms;
   int32_t candidates;
+  int32_t algorithm;      /* MCG_ALGO_HISTORY or MCG_ALGO_EVENT */
+  int32_t steps_per_pass; /* event mode: events per pass */
 } mcg_batch_tuning;
 int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_batch_tuning *out);
+
+/* History-based (default: the persistent launch above) or event-based
+ * batched runs: all slabs' particles in one structure-of-arrays bank, K
+ * events per pass (0: 8).  Identical tallies. */
+int mcg_batch_set_algorithm(mcg_context *ctx, int32_t algorithm, int32_t steps_per_pass);
 
 /* ---- Differentiation: forward tally + adjoint gradients of a tally loss ----
  * Loss F = sum_c w_c a_c over the chain cells, a_c the weight absorbed in

@@ -50,7 +50,8 @@ class Slab(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("block", C.c_int32), ("tally_mode", C.c_int32), ("item_histories", C.c_int64),
-                ("sample_ms", C.c_float), ("candidates", C.c_int32)]
+                ("sample_ms", C.c_float), ("candidates", C.c_int32), ("algorithm", C.c_int32),
+                ("steps_per_pass", C.c_int32)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -118,6 +119,7 @@ def load_library(path=None):
         "mcg_batch_tally_read": (C.c_int, [vp, vp, vp]),
         "mcg_batch_set_launch": (C.c_int, [vp, i32, i64, i32]),
         "mcg_batch_autotune": (C.c_int, [vp, C.c_double, C.POINTER(Tuning)]),
+        "mcg_batch_set_algorithm": (C.c_int, [vp, i32, i32]),
         "mcg_libm_eval_device": (C.c_int, [vp, C.c_int, vp, vp, i64]),
         "mcg_verify_division": (C.c_int, [vp, C.c_int, C.c_uint64] + [C.POINTER(C.c_uint64)] * 3),
     }
@@ -374,6 +376,10 @@ class Context:
 
     def batch_set_launch(self, block=0, item_histories=0, tally_mode=-1):
         _check(self.lib.mcg_batch_set_launch(self.h, block, item_histories, tally_mode))
+
+    def batch_set_algorithm(self, algorithm="history", steps_per_pass=0):
+        _check(self.lib.mcg_batch_set_algorithm(self.h, 0 if algorithm == "history" else 1,
+                                                int(steps_per_pass)))
 
     def batch_autotune(self, sample_fraction=0.02):
         t = Tuning()

@@ -23,11 +23,6 @@
 #include "mcg_internal.h"
 #include "mcg_track.cuh"
 
-struct mcg_batch_slab_dev {
-  int32_t cell_off, m;
-  mcg_source src;
-};
-
 struct mcg_batch_item {
   int32_t slab, pad;
   int64_t first, count;
@@ -229,7 +224,7 @@ static mcg_batch_state *batch_of(mcg_context *ctx)
 static void batch_free(mcg_batch_state *B)
 {
   for (void *p : {B->d_slabs, B->d_items, (void *)B->d_cells_strict, (void *)B->d_cells_fast,
-                  (void *)B->d_tally, (void *)B->d_item_next})
+                  (void *)B->d_tally, (void *)B->d_item_next, (void *)B->d_hist0})
     if (p)
       cudaFree(p);
   if (B->graph)
@@ -428,6 +423,46 @@ static int batch_enqueue(mcg_context *ctx, mcg_batch_state *B, const mcg_batch_l
   return MCG_OK;
 }
 
+/* First history of each slab for the event engine, with the same sampled
+ * history counts as build_items at this fraction; returns the total. */
+static int build_hist0(mcg_batch_state *B, double fraction, unsigned long long *total)
+{
+  std::vector<unsigned long long> h0(B->n_slabs);
+  unsigned long long t = 0;
+  for (int s = 0; s < B->n_slabs; ++s) {
+    int64_t n = B->slabs[s].n_histories;
+    if (fraction < 1.0)
+      n = std::max<int64_t>(std::min<int64_t>(n, 32), (int64_t)std::ceil(n * fraction));
+    h0[s] = t;
+    t += (unsigned long long)n;
+  }
+  *total = t;
+  if (B->hist0_fraction == fraction && B->d_hist0)
+    return MCG_OK;
+  cudaError_t e = cudaSuccess;
+  if (!B->d_hist0)
+    e = cudaMalloc(&B->d_hist0, (size_t)B->n_slabs * sizeof(unsigned long long));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(B->d_hist0, h0.data(), h0.size() * sizeof(unsigned long long),
+                   cudaMemcpyHostToDevice);
+  if (e != cudaSuccess)
+    return mcg_cuda_fail(e, "mcg_batch: slab history offsets");
+  B->hist0_fraction = fraction;
+  return MCG_OK;
+}
+
+/* One batched run with the event engine (histories at this fraction). */
+static int batch_run_event(mcg_context *ctx, mcg_batch_state *B, double fraction, int steps)
+{
+  unsigned long long total = 0;
+  int rc = build_hist0(B, fraction, &total);
+  if (rc != MCG_OK)
+    return rc;
+  const bool strict = ctx->mode == MCG_MODE_STRICT;
+  return mcg_event_run_slabs(ctx, strict ? B->d_cells_strict : B->d_cells_fast, B->d_tally,
+                             B->d_slabs, B->d_hist0, B->n_slabs, total, B->min_w, steps);
+}
+
 static int batch_prepare(mcg_context *ctx, mcg_batch_state **out)
 {
   if (!ctx || !ctx->ext || ctx->ext->batch.n_slabs == 0)
@@ -446,6 +481,11 @@ extern "C" int mcg_batch_run(mcg_context *ctx)
   int rc = batch_prepare(ctx, &B);
   if (rc != MCG_OK)
     return rc;
+  if (B->algorithm == MCG_ALGO_EVENT) {
+    if ((rc = batch_run_event(ctx, B, 1.0, B->event_steps)) != MCG_OK)
+      return rc;
+    return mcg_sync(ctx);
+  }
   if (B->items_built_for != (int)B->item_histories) {
     if ((rc = build_items(ctx, B, B->item_histories, 1.0)) != MCG_OK)
       return rc;
@@ -611,6 +651,16 @@ extern "C" int mcg_batch_set_launch(mcg_context *ctx, int32_t block, int64_t ite
   return MCG_OK;
 }
 
+extern "C" int mcg_batch_set_algorithm(mcg_context *ctx, int32_t algorithm, int32_t steps_per_pass)
+{
+  if (!ctx || (algorithm != MCG_ALGO_HISTORY && algorithm != MCG_ALGO_EVENT) || steps_per_pass < 0)
+    return mcg_fail(MCG_ERR_ARG, "mcg_batch_set_algorithm: bad arguments");
+  mcg_batch_state *B = batch_of(ctx);
+  B->algorithm = algorithm;
+  B->event_steps = steps_per_pass ? steps_per_pass : 8;
+  return MCG_OK;
+}
+
 extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_batch_tuning *out)
 {
   mcg_batch_state *B;
@@ -624,7 +674,8 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
   const int tmodes[] = {MCG_TALLY_SMEM32, MCG_TALLY_SMEM64};
   float best = 1e30f;
   int nc = 0;
-  mcg_batch_tuning pick = {B->block, B->tally_mode, B->item_histories, 0.f, 0};
+  mcg_batch_tuning pick = {B->block, B->tally_mode, B->item_histories, 0.f, 0, MCG_ALGO_HISTORY,
+                           0};
   bool warmed = false;
   for (int64_t it : items) {
     /* the sample keeps the full run's number of items per slab, so the
@@ -651,10 +702,25 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
         ++nc;
         if (ctx->last_ms < best) {
           best = ctx->last_ms;
-          pick = {bl, tm, it, best, 0};
+          pick = {bl, tm, it, best, 0, MCG_ALGO_HISTORY, 0};
         }
       }
   }
+  /* the event-based form on the same sample */
+  for (int k : {4, 16}) {
+    for (int rep = 0; rep < 2; ++rep) /* the first run sizes the bank */
+      if ((rc = batch_run_event(ctx, B, sample_fraction, k)) != MCG_OK ||
+          (rc = mcg_sync(ctx)) != MCG_OK)
+        return rc;
+    ++nc;
+    if (ctx->last_ms < best) {
+      best = ctx->last_ms;
+      pick = {B->block, B->tally_mode, B->item_histories, best, 0, MCG_ALGO_EVENT, k};
+    }
+  }
+  B->algorithm = pick.algorithm;
+  if (pick.algorithm == MCG_ALGO_EVENT)
+    B->event_steps = pick.steps_per_pass;
   B->block = pick.block;
   B->tally_mode = pick.tally_mode;
   B->item_histories = pick.item_histories;

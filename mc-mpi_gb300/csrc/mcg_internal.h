@@ -30,6 +30,10 @@ struct mcg_batch_state {
   /* launch shape, chosen by mcg_batch_set_launch or the autotuner */
   int block = 512, tally_mode = 1;
   int64_t item_histories = 16384;
+  /* history- or event-based; events per pass of the event engine */
+  int algorithm = MCG_ALGO_HISTORY, event_steps = 8;
+  unsigned long long *d_hist0 = nullptr; /* first history of each slab (event mode) */
+  double hist0_fraction = -1.0;          /* fraction of the histories d_hist0 is for */
   /* CUDA graph of one run (memset of the item counter + the kernel) */
   cudaGraphExec_t graph = nullptr;
   bool graph_valid = false;
@@ -53,11 +57,29 @@ struct mcg_ext {
   mcg_fit_state *fit = nullptr;
 };
 
-/* Structure-of-arrays particle buffer of the event-based tracker. */
+/* Structure-of-arrays particle buffer of the event-based tracker: per
+ * particle the state, the cell index local to its chain or slab, the history
+ * (chain) or slab (batched) it belongs to, its step and scatter counts, and
+ * in the collision queue the flight sample already drawn. */
 struct mcg_soa {
   unsigned long long *seed;
   float *x, *mu, *wmc;
   int32_t *idx, *hid, *nst, *nsc;
+  float *h;
+};
+
+/* Counters of the event engine, on the device. */
+struct mcg_ev_ctl {
+  unsigned long long n_in, n_out, n_q;     /* particles in the bank, out, in the queue */
+  unsigned long long next, total;          /* histories born so far, of the run */
+  unsigned long long birth_base, birth_n;  /* this pass's newborns: slots, count */
+  unsigned long long birth_first, passes;
+};
+
+/* One slab of the batched form (and of the event engine's slab mode). */
+struct mcg_batch_slab_dev {
+  int32_t cell_off, m;
+  mcg_source src;
 };
 
 struct mcg_context {
@@ -99,10 +121,10 @@ struct mcg_context {
 
   /* algorithm: history-based (default) or event-based with K events per pass */
   int algorithm = MCG_ALGO_HISTORY, event_steps = 1, event_passes = 0;
-  mcg_soa event_buf[2] = {};
+  mcg_soa event_buf[3] = {}; /* bank in, bank out, collision queue */
   size_t event_cap = 0;
   std::vector<void *> event_owned;
-  unsigned *event_count = nullptr;
+  mcg_ev_ctl *event_ctl = nullptr;
 
   std::vector<void *> owned; /* device allocations freed at destroy */
   mcg_ext *ext = nullptr;
@@ -119,5 +141,8 @@ int mcg_load_libm(mcg_context *ctx);
 extern "C" int mcg_fit_release(mcg_context *ctx);
 struct mcg_track_params;
 int mcg_event_run(mcg_context *ctx, mcg_track_params &P);
+int mcg_event_run_slabs(mcg_context *ctx, const float4 *cells, unsigned long long *tally,
+                        const void *slabs, const unsigned long long *slab_hist0, int n_slabs,
+                        unsigned long long total, float min_w, int steps_per_pass);
 
 #endif

@@ -224,6 +224,175 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
   idx = inew;
 }
 
+/* One Layer::particle_step (src/layer.cpp:123-190) on a lane's particle in
+ * cell c = {sig_a, sig_i or -ln2/sig_i, edge_lo, edge_hi}, in two parts, for
+ * the event-based tracker: mcg_step_cross draws the flight sample h and
+ * completes the step when it is a certain crossing (STRICT: the branch-free
+ * path of mcg_step; FAST: the flight ends past the edge), returning true;
+ * otherwise it changes nothing but the seed and returns false, and
+ * mcg_step_rest completes the step from h.  Together they perform exactly
+ * mcg_step's operations (mcg_step, the one-piece form above, serves the
+ * history-based kernels, where the split costs about 6 %).  STRICT: the reference's float operations and host-libm
+ * logf/expf; the crossing's absorption is computed before the logarithm and
+ * a certified exponential bound settles most crossings without it (see
+ * MCG_CROSS_FACTOR).  FAST: hardware log2/exp2.  Deposits go into
+ * *tally_cell; l_out/coll_out/dep_out (adjoint) receive the flight length,
+ * whether it ended in a collision and the deposit. */
+template <bool STRICT, int TALLY>
+__device__ __forceinline__ bool mcg_step_cross(uint64_t &seed, float &x, float &mu, float &wmc,
+                                               float &inv_mu, int &idx, const float4 c,
+                                               unsigned long long *tally_cell, int qs,
+                                               const mcg_libm_tab *T, const mcg_libm_dev &LM,
+                                               float &h, float *l_out = nullptr,
+                                               bool *coll_out = nullptr, float *dep_out = nullptr)
+{
+  const float sig_a = c.x;
+  h = STRICT ? mcg_rnd_real(seed) : mcg_rnd_real_fast(seed);
+  const bool neg = mu < 0.0f;
+  const float edge = neg ? c.z : c.w;
+  if (STRICT) {
+    /* The certain crossing, computed without branches: d_edge by the cached
+     * reciprocal, the crossing's absorption by the exp evaluator, and the
+     * certified bound.  It is the reference's step exactly when every
+     * condition in `easy` holds (division and exp arguments in the range
+     * where those forms are exact, no exception-table candidate, a flight
+     * certainly past the edge); almost every step of a fine mesh is such a
+     * crossing. */
+    const float a = __fsub_rn(edge, x), aa = fabsf(a);
+    const float de_q = mcg_div_by_rcp(a, mu, inv_mu);
+    const float t_q = __fmul_rn(-sig_a, de_q);
+    float d_q;
+    const float y_q = mcg_exp_ff_core(t_q, &d_q, T);
+    const float bound_q = __fmul_rn(
+        mcg_ex2_approx(__fmul_rn(__fmul_rn(c.y, de_q), -MCG_LOG2E_F)), MCG_CROSS_FACTOR);
+    const bool easy = (inv_mu != 0.0f) & (aa >= 0x1p-100f) & (aa <= 0x1p100f) &
+                      (t_q >= MCG_EXP_ONE_BOUND) & (t_q < 89.0f) & (d_q > LM.tau_exp_max) &
+                      (c.y > MCG_EPS) & (h < bound_q);
+    if (!easy)
+      return false;
+    x = edge;
+    const float dw = __fmul_rn(__fsub_rn(1.0f, y_q), wmc);
+    wmc = __fsub_rn(wmc, dw);
+    if (tally_cell)
+      mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dw, qs));
+    if (l_out) {
+      *l_out = de_q;
+      *coll_out = false;
+      *dep_out = dw;
+    }
+  } else {
+    const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
+    const float di = c.y != 0.0f ? __log2f(h) * c.y : MCG_MAXREAL;
+    if (di < de)
+      return false;
+    if (l_out) {
+      *l_out = de;
+      *coll_out = false;
+    }
+    const float om = mcg_one_minus_exp_fast(-sig_a * de);
+    x = edge;
+    /* deposit the weight actually removed (exact by Sterbenz while the new
+     * weight is at least half the old), so the tally plus the surviving
+     * weights conserve the born weight to the fixed-point resolution */
+    const float wnew = __fsub_rn(wmc, __fmul_rn(om, wmc));
+    const float dep = __fsub_rn(wmc, wnew);
+    wmc = wnew;
+    if (tally_cell)
+      mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dep, qs));
+    if (dep_out)
+      *dep_out = dep;
+  }
+  idx = neg ? idx - 1 : idx + 1;
+  return true;
+}
+
+template <bool STRICT, int TALLY>
+__device__ __forceinline__ void mcg_step_rest(float h, uint64_t &seed, float &x, float &mu,
+                                              float &wmc, float &inv_mu, int &idx, uint32_t &nsc,
+                                              const float4 c, unsigned long long *tally_cell,
+                                              int qs, const mcg_libm_tab *T,
+                                              const mcg_libm_dev &LM, float *l_out = nullptr,
+                                              bool *coll_out = nullptr, float *dep_out = nullptr)
+{
+  const float sig_a = c.x;
+  const bool neg = mu < 0.0f;
+  int inew = neg ? idx - 1 : idx + 1;
+  const float edge = neg ? c.z : c.w;
+  float om;
+  if (STRICT) {
+    /* d_edge, and the crossing's absorption, do not depend on the flight
+     * sample: start them before the logarithm */
+    const float a = __fsub_rn(edge, x), aa = fabsf(a);
+    const float de = inv_mu == 0.0f ? MCG_MAXREAL
+                     : (aa >= 0x1p-100f && aa <= 0x1p100f) ? mcg_div_by_rcp(a, mu, inv_mu)
+                                                            : __fdiv_rn(a, mu);
+    const float om_cross = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, de), T, LM);
+    /* di = sig_i > EPS ? -log(h) / sig_i : MAXREAL; the exact value is
+     * only needed when the flight may end inside the cell: the certified
+     * test h < ~exp(-sig_i de) settles almost every crossing */
+    bool cross = true;
+    float di = MCG_MAXREAL;
+    if (c.y > MCG_EPS) {
+      const float bound = __fmul_rn(
+          mcg_ex2_approx(__fmul_rn(__fmul_rn(c.y, de), -MCG_LOG2E_F)), MCG_CROSS_FACTOR);
+      if (!(h < bound)) {
+        di = __fdiv_rn(-mcg_logf_strict(h, T, LM), c.y);
+        cross = !(di < de);
+      }
+    } else {
+      cross = !(di < de);
+    }
+    if (!cross) {
+      inew = idx;
+      x = __fadd_rn(x, __fmul_rn(di, mu));
+      mu = __fsub_rn(__fmul_rn(2.0f, mcg_rnd_real(seed)), 1.0f);
+      inv_mu = mcg_flight_rcp(mu);
+      om = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, di), T, LM);
+      ++nsc;
+    } else {
+      x = edge;
+      om = om_cross;
+    }
+    const float dw = __fmul_rn(om, wmc);
+    wmc = __fsub_rn(wmc, dw);
+    if (tally_cell)
+      mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dw, qs));
+    if (l_out) {
+      *l_out = cross ? de : di;
+      *coll_out = !cross;
+      *dep_out = dw;
+    }
+  } else {
+    const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
+    const float om_cross = mcg_one_minus_exp_fast(-sig_a * de);
+    const float di = c.y != 0.0f ? __log2f(h) * c.y : MCG_MAXREAL;
+    const bool coll = di < de;
+    if (l_out) {
+      *l_out = coll ? di : de;
+      *coll_out = coll;
+    }
+    if (coll) {
+      inew = idx;
+      x = fmaf(di, mu, x);
+      mu = fmaf(2.0f, mcg_rnd_real_fast(seed), -1.0f);
+      inv_mu = mcg_flight_rcp(mu);
+      om = mcg_one_minus_exp_fast(-sig_a * di);
+      ++nsc;
+    } else {
+      x = edge;
+      om = om_cross;
+    }
+    const float wnew = __fsub_rn(wmc, __fmul_rn(om, wmc));
+    const float dep = __fsub_rn(wmc, wnew);
+    wmc = wnew;
+    if (tally_cell)
+      mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dep, qs));
+    if (dep_out)
+      *dep_out = dep;
+  }
+  idx = inew;
+}
+
 template <bool STRICT, int TALLY>
 __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
 {

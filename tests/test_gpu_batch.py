@@ -70,3 +70,24 @@ def test_batch_autotune_keeps_parity(mcg, small_batch):
         assert t["candidates"] >= 6 and t["block"] in (256, 512, 1024)
         ctx.batch_run()
         assert np.array_equal(ctx.batch_tally_q(), ref)
+
+
+@pytest.mark.parametrize("mode", ["strict", "fast"])
+@pytest.mark.parametrize("k", [1, 8])
+def test_batch_event_mode_equals_history(mcg, small_batch, mode, k):
+    """The event-based batched form (all slabs' particles in one bank, K
+    events per pass) gives the history-based form's tallies and counters."""
+    slabs, sigs, rates = small_batch
+    with mcg.Context(mode=mode) as ctx:
+        ctx.set_tally_scale(40)
+        ctx.batch_set(slabs, sigs, rates, 1e-12)
+        ctx.batch_run()
+        ref, c_ref = ctx.batch_tally_q(), ctx.counters()
+        ctx.batch_tally_reset()
+        ctx.batch_set_algorithm("event", k)
+        ctx.batch_run()
+        assert np.array_equal(ctx.batch_tally_q(), ref)
+        c = ctx.counters()
+        for key in ("histories", "steps", "scatters", "leaked_left", "leaked_right", "killed",
+                    "w_left_q", "w_right_q", "w_killed_q", "error_flags"):
+            assert c[key] == c_ref[key], key

@@ -301,6 +301,26 @@ def test_event_mode_identical_to_history(mcg, oracle, mode, k):
         assert ctx.counters() == ca
 
 
+@pytest.mark.parametrize("k", [1, 4])
+def test_event_mode_edge_cases(ctx, mcg, k):
+    """The event-based tracker on the reference's edge-case traces: per
+    particle bit-exact, like the history tracker."""
+    g = load("traces_edge.npz")
+    lt = g["layer"]
+    ctx.set_layers([int(lt[3])], [int(lt[4])], [f32(lt[2])], g["sigs"], g["rates"],
+                   float(g["min_w"]))
+    ctx.set_algorithm("event", k)
+    try:
+        p = g["initial"].astype(mcg.PARTICLE_DTYPE).copy()
+        r = ctx.simulate(p)
+    finally:
+        ctx.set_algorithm("history", 1)
+    assert p.tobytes() == g["final"].astype(mcg.PARTICLE_DTYPE).tobytes()
+    assert np.array_equal(r["results"], g["result"])
+    assert np.array_equal(r["steps"], g["steps"])
+    assert np.array_equal(r["scatters"], g["scatters"])
+
+
 @pytest.mark.parametrize("per_cycle", [500, 65536])
 def test_worker_handover_queues_match_fused(mcg, per_cycle):
     """The workers' cycle with per-sub-domain queues (64 sub-domains) gives
