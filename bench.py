@@ -388,7 +388,7 @@ def bench_batched(mcg, mode, device, scale=0.02, reps=2):
                         f"sigma_s~U[0,10], histories log-uniform [1e3,1e6] x {scale}"}
 
 
-def bench_event(mcg, mode, device, st, m, dx, sigs, rates, n=10_000_000, k=4):
+def bench_event(mcg, mode, device, st, m, dx, sigs, rates, n=10_000_000, k=16):
     """The event-based tracker (SoA particle bank, K events per pass, per
     event type compaction) on the first n histories of the workload, against
     the history-based tracker on the same histories (identical tallies)."""
