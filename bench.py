@@ -323,6 +323,8 @@ def run_gpu(args):
                            "peak_gops": sms * 128 * f_sm / 1e9, "frac": issue_frac},
         "clocks": clocks,
     }
+    if rank == 0 and not args.no_extra:
+        line["fom"] = figure_of_merit(ctx, value / ws)
     if rank == 0 and not args.no_extra and args.algorithm == "history":
         line["event"] = bench_event(mcg, args.mode, local, st, m, dx, sigs, rates)
     if rank == 0 and not args.no_extra and args.mode == "strict":
@@ -386,6 +388,30 @@ def bench_batched(mcg, mode, device, scale=0.02, reps=2):
             "steps_per_s": steps / t, "histories": n, "launches": 1,
             "workload": f"4096 slabs, cells U{{16..4096}}, L~U[0.5,5], sigma_a~U[0.1,5], "
                         f"sigma_s~U[0,10], histories log-uniform [1e3,1e6] x {scale}"}
+
+
+def figure_of_merit(ctx, hist_per_s, n_batches=20, size=100_000):
+    """FOM = 1 / (SE^2 T) of the per-cell tally at this throughput: the
+    per-history variance of each cell's absorbed weight comes from
+    n_batches independent batches (disjoint histories of the same source)
+    run on the GPU; SE^2 = var / N and T = N / (histories/s), so
+    FOM = (histories/s) / var.  Reported averaged over the visited cells,
+    and as the relative-error form (mean^2 / var, MCNP's figure of merit)
+    as a median over them.  The reference's estimator is the same, so the
+    two arms' FOM ratio equals their throughput ratio."""
+    means = []
+    for b in range(n_batches):
+        ctx.tally_reset()
+        ctx.simulate_source(N_TOTAL + b * size, size)
+        means.append(ctx.tally() / size)
+    ctx.tally_reset()
+    M = np.array(means)
+    var = M.var(axis=0, ddof=1) * size
+    mu = M.mean(axis=0)
+    seen = var > 0
+    return {"value": float(np.mean(hist_per_s / var[seen])), "unit": "1/s (1/(SE^2 T), mean over cells)",
+            "relative_median": float(np.median(hist_per_s * mu[seen] ** 2 / var[seen])),
+            "cells": int(seen.sum()), "variance_from": f"{n_batches} batches of {size} histories"}
 
 
 def bench_event(mcg, mode, device, st, m, dx, sigs, rates, n=10_000_000, k=16):
