@@ -164,7 +164,10 @@ MCG_HD float mcg_exp_ff_core(float t, float *delta, const mcg_libm_tab *T)
     /* |t| <= ln2/128: e^t = (1 + t) + t^2 (1/2 + t/6 + t^2/24), the first
      * sum exact as a float-float (Fast2Sum), the tail within 2^-38.  Less
      * accurate than the general path, which the exception table absorbs:
-     * its generator runs this same code over every argument. */
+     * its generator runs this same code over every argument.  The two paths
+     * are therefore not interchangeable: which one evaluates an argument
+     * must depend on the argument alone (never, say, on the other lanes of
+     * a warp), or results leave the table's cover. */
     float p = MCG_FMA(t, MCG_EXP_Q4, MCG_EXP_Q3);
     p = MCG_FMA(t, p, 0.5f);
     float r2 = MCG_MUL(MCG_MUL(t, t), p);
