@@ -244,10 +244,12 @@ int mcg_batch_tally_read(mcg_context *ctx, int64_t *h_q, double *h_f64);
 int mcg_batch_set_launch(mcg_context *ctx, int32_t block, int64_t item_histories,
                          int32_t tally_mode);
 /* Autotuner: times every candidate on a sample of each slab's histories
- * (fraction in (0, 1]): the history-based launch shapes (block, histories
- * per work item, tally privatisation) and the event-based form at 4 and 16
- * events per pass, and keeps the fastest.  Reports the choice and its sample
- * time; the batch tally and counters are reset afterwards. */
+ * (fraction in (0, 1], raised so that the sample holds at least four times
+ * the event engine's drain size, or the whole run): the history-based
+ * launch shapes (block, histories per work item, tally privatisation) and
+ * the event-based form at 4 and 16 events per pass, and keeps the one with
+ * the least time per history.  Reports the choice and its sample time; the
+ * batch tally and counters are reset afterwards. */
 typedef struct mcg_batch_tuning {
   int32_t block;
   int32_t tally_mode;

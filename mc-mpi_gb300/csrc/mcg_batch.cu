@@ -672,7 +672,20 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
   const int blocks[] = {256, 512, 1024};
   const int64_t items[] = {4096, 16384, 65536};
   const int tmodes[] = {MCG_TALLY_SMEM32, MCG_TALLY_SMEM64};
-  float best = 1e30f;
+  /* every candidate runs the same sample, of at least four times the event
+   * engine's drain size (below it the event-based form is a single drain
+   * launch, and a persistent launch is dominated by its tail), or the whole
+   * run; candidates compete on time per history */
+  unsigned long long n_full = 0, n_hist = 0;
+  if ((rc = build_hist0(B, 1.0, &n_full)) != MCG_OK)
+    return rc;
+  sample_fraction = std::min(
+      1.0, std::max(sample_fraction, 4.0 * (double)mcg_event_drain_below(ctx) / (double)n_full));
+  if ((rc = build_hist0(B, sample_fraction, &n_hist)) != MCG_OK)
+    return rc;
+  const double f_event = sample_fraction;
+  const unsigned long long n_event = n_hist;
+  double best = 1e30; /* ms per history */
   int nc = 0;
   mcg_batch_tuning pick = {B->block, B->tally_mode, B->item_histories, 0.f, 0, MCG_ALGO_HISTORY,
                            0};
@@ -700,22 +713,21 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
         }
         warmed = true;
         ++nc;
-        if (ctx->last_ms < best) {
-          best = ctx->last_ms;
-          pick = {bl, tm, it, best, 0, MCG_ALGO_HISTORY, 0};
+        if (ctx->last_ms / (double)n_hist < best) {
+          best = ctx->last_ms / (double)n_hist;
+          pick = {bl, tm, it, ctx->last_ms, 0, MCG_ALGO_HISTORY, 0};
         }
       }
   }
-  /* the event-based form on the same sample */
+  /* the event-based form */
   for (int k : {4, 16}) {
     for (int rep = 0; rep < 2; ++rep) /* the first run sizes the bank */
-      if ((rc = batch_run_event(ctx, B, sample_fraction, k)) != MCG_OK ||
-          (rc = mcg_sync(ctx)) != MCG_OK)
+      if ((rc = batch_run_event(ctx, B, f_event, k)) != MCG_OK || (rc = mcg_sync(ctx)) != MCG_OK)
         return rc;
     ++nc;
-    if (ctx->last_ms < best) {
-      best = ctx->last_ms;
-      pick = {B->block, B->tally_mode, B->item_histories, best, 0, MCG_ALGO_EVENT, k};
+    if (ctx->last_ms / (double)n_event < best) {
+      best = ctx->last_ms / (double)n_event;
+      pick = {B->block, B->tally_mode, B->item_histories, ctx->last_ms, 0, MCG_ALGO_EVENT, k};
     }
   }
   B->algorithm = pick.algorithm;

@@ -579,7 +579,7 @@ static int ev_run_t(mcg_context *ctx, mcg_ev_params &P, unsigned long long total
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, mcg_ev_flight_kernel<STRICT, SLABS, SMEM>,
                                                 MCG_EV_BLOCK, smem);
   const int grid = ctx->sm_count * std::max(bps, 1);
-  const unsigned long long drain_below = (unsigned long long)ctx->sm_count * 1024;
+  const unsigned long long drain_below = mcg_event_drain_below(ctx);
   mcg_soa cur = ctx->event_buf[0], other = ctx->event_buf[1];
   P.q = ctx->event_buf[2];
   cudaEventRecord(ctx->ev0, ctx->stream);

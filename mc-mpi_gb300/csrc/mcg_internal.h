@@ -140,6 +140,12 @@ void mcg_ext_destroy(mcg_context *ctx);
 int mcg_load_libm(mcg_context *ctx);
 extern "C" int mcg_fit_release(mcg_context *ctx);
 struct mcg_track_params;
+/* Below this many live particles (once the source is exhausted) the event
+ * engine finishes the run with one history-based launch. */
+inline unsigned long long mcg_event_drain_below(const mcg_context *ctx)
+{
+  return (unsigned long long)ctx->sm_count * 1024;
+}
 int mcg_event_run(mcg_context *ctx, mcg_track_params &P);
 int mcg_event_run_slabs(mcg_context *ctx, const float4 *cells, unsigned long long *tally,
                         const void *slabs, const unsigned long long *slab_hist0, int n_slabs,
