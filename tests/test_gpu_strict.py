@@ -189,6 +189,29 @@ def test_simulate_pinned_buffers_in_place(ctx, mcg, oracle):
     assert np.array_equal(ctx.tally_q(), q0)
 
 
+@pytest.mark.parametrize("mode", ["strict", "fast"])
+def test_tally_independent_of_launch_shape(mcg, oracle, mode):
+    """The fixed-point tally is a sum of integers: every launch shape (block
+    size, blocks per SM, refill interval) and tally privatisation (64-bit
+    shared, 32-bit shared with carry, global) gives the same bits and the
+    same counters."""
+    st, m, dx, sigs, rates = _slab(mcg, 2000, 16)
+    with mcg.Context(mode=mode) as ctx:
+        ctx.set_layers(st, m, dx, sigs, rates, 1e-12)
+        ref = ref_c = None
+        for block, bps, refill in ((0, 0, 0), (256, 2, 1), (1024, 1, 32), (512, 0, 8)):
+            for tmode in (0, 1, 2):
+                ctx.set_launch(block, bps, refill)
+                ctx.set_tally_mode(tmode)
+                ctx.tally_reset()
+                ctx.simulate_source(0, 20000)
+                q, c = ctx.tally_q(), ctx.counters()
+                if ref is None:
+                    ref, ref_c = q, c
+                assert np.array_equal(q, ref), (block, bps, refill, tmode)
+                assert c == ref_c, (block, bps, refill, tmode)
+
+
 def test_rnd_real_device_kat(ctx, oracle):
     """src/test_curandom.cu: device rnd_real == CPU, seeds and floats."""
     import torch
