@@ -9,8 +9,9 @@
  * rounded result on about 2e5 inputs each, always by one unit in the last
  * place and always for inputs whose exact result lies near a midpoint.  The
  * strict GPU tracker must reproduce the host library bit for bit, so it:
- *   1. evaluates log/exp here to ~2^-45 relative accuracy (float-float),
- *      which equals the correctly rounded value except in rare hard cases;
+ *   1. evaluates log here to ~2^-45 and exp to ~2^-37 relative accuracy
+ *      (float-float), which equals the correctly rounded value except in
+ *      rare hard cases;
  *   2. measures delta = distance of the float-float value from the nearest
  *      rounding midpoint, in units of the local float spacing (0 .. 0.5);
  *   3. if delta is at most the per-bucket threshold tau (computed by the
@@ -155,71 +156,94 @@ MCG_HD float mcg_log_ff(float x, float *delta, const mcg_libm_tab *T)
   return yh;
 }
 
-/* exp(t) for -17.5 <= t < 89 (other arguments give meaningless values,
- * and touch nothing outside T). */
-MCG_HD float mcg_exp_ff_core(float t, float *delta, const mcg_libm_tab *T)
+/* e^(rh + rl) for |rh| <= ln2/128, |rl| <= ulp(rh): (1 + rh) as an exact
+ * float-float (Fast2Sum) plus rh^2 (1/2 + rh/6 + rh^2/24) + rl, within
+ * 2^-38 relative; returns the rounded value, *yl the float-float remainder.
+ * With rl = 0 (the small-argument path) the added rl changes nothing. */
+MCG_HD float mcg_exp_small_form(float rh, float rl, float *yl)
 {
-  int k = mcg_rint_k(MCG_MUL(t, MCG_EXP_INV));
-  if (k == 0) {
-    /* |t| <= ln2/128: e^t = (1 + t) + t^2 (1/2 + t/6 + t^2/24), the first
-     * sum exact as a float-float (Fast2Sum), the tail within 2^-38.  Less
-     * accurate than the general path, which the exception table absorbs:
-     * its generator runs this same code over every argument.  The two paths
-     * are therefore not interchangeable: which one evaluates an argument
-     * must depend on the argument alone (never, say, on the other lanes of
-     * a warp), or results leave the table's cover. */
-    float p = MCG_FMA(t, MCG_EXP_Q4, MCG_EXP_Q3);
-    p = MCG_FMA(t, p, 0.5f);
-    float r2 = MCG_MUL(MCG_MUL(t, t), p);
-    float s = MCG_ADD(1.0f, t);
-    float se = MCG_SUB(t, MCG_SUB(s, 1.0f));
-    float lo = MCG_ADD(se, r2);
-    float yh = MCG_ADD(s, lo);
-    float yl = MCG_ADD(MCG_SUB(s, yh), lo);
-    /* distance from the rounding midpoint in units of 2^-24, the float
-     * spacing below 1 (every t < 0); above 1 the spacing is 2^-23 and this
-     * measure is only a filter key, which the table generator, running this
-     * same code, sets its thresholds by */
-    *delta = MCG_SUB(0.5f, MCG_MUL(fabsf(yl), 16777216.0f));
-    return yh;
-  }
-  float kf = mcg_int_to_float(k);
-  float p1 = MCG_MUL(kf, MCG_EXP_C1); /* exact */
-  float r1 = MCG_SUB(t, p1);           /* exact */
-  float p2 = MCG_MUL(kf, MCG_EXP_C2);
-  float p2e = MCG_FMA(kf, MCG_EXP_C2, -p2);
+  float p = MCG_FMA(rh, MCG_EXP_Q4, MCG_EXP_Q3);
+  p = MCG_FMA(rh, p, 0.5f);
+  const float r2 = MCG_MUL(MCG_MUL(rh, rh), p);
+  const float s = MCG_ADD(1.0f, rh);
+  const float se = MCG_SUB(rh, MCG_SUB(s, 1.0f));
+  const float lo = MCG_ADD(MCG_ADD(se, r2), rl);
+  const float yh = MCG_ADD(s, lo);
+  *yl = MCG_ADD(MCG_SUB(s, yh), lo);
+  return yh;
+}
+
+/* Midpoint distance of the small-argument path, in units of 2^-24, the float
+ * spacing below 1 (every t < 0); above 1 the spacing is 2^-23 and this
+ * measure is only a filter key, which the table generator, running this
+ * same code, sets its thresholds by. */
+MCG_HD float mcg_exp_small_delta(float yl)
+{
+  return MCG_SUB(0.5f, MCG_MUL(fabsf(yl), 16777216.0f));
+}
+
+/* exp(t), k = rint(t 64 / ln2) == 0: the small-argument path. */
+MCG_HD float mcg_exp_ff_small(float t, float *delta)
+{
+  float yl;
+  const float yh = mcg_exp_small_form(t, 0.0f, &yl);
+  *delta = mcg_exp_small_delta(yl);
+  return yh;
+}
+
+/* exp(t), any k: t = k ln2/64 + r (r as a float-float), e^r by the small
+ * form, times 2^(j/64) (a float-float table entry, j = k mod 64), times
+ * 2^((k - j)/64).  For k == 0 every step is exact or an exact identity (r
+ * = t, rl = 0, table entry 1 + 0, scale 1) and the midpoint measure is the
+ * small path's, so this path returns the small path's bits: the two are
+ * interchangeable (kernels may choose the path per warp), which the GPU
+ * tests check over every argument. */
+MCG_HD float mcg_exp_ff_general(float t, int k, float *delta, const mcg_libm_tab *T)
+{
+  const float kf = mcg_int_to_float(k);
+  const float p1 = MCG_MUL(kf, MCG_EXP_C1); /* exact */
+  const float r1 = MCG_SUB(t, p1);           /* exact */
+  const float p2 = MCG_MUL(kf, MCG_EXP_C2);
+  const float p2e = MCG_FMA(kf, MCG_EXP_C2, -p2);
   /* r = r1 - p2 (TwoSum) - p2e - k*C3 */
-  float rh0 = MCG_SUB(r1, p2);
-  float bv = MCG_SUB(rh0, r1);
-  float re = MCG_SUB(MCG_SUB(r1, MCG_SUB(rh0, bv)), MCG_ADD(p2, bv));
-  float rl0 = MCG_SUB(MCG_SUB(re, p2e), MCG_MUL(kf, MCG_EXP_C3));
-  float rh = MCG_ADD(rh0, rl0);
-  float rl = MCG_ADD(MCG_SUB(rh0, rh), rl0);
-  /* e^r - 1 = sh + sl */
-  float q2h = MCG_MUL(rh, rh);
-  float q2l = MCG_FMA(rh, rh, -q2h);
-  float h2h = MCG_MUL(0.5f, q2h);
-  float sh = MCG_ADD(rh, h2h);
-  float sl = MCG_ADD(MCG_SUB(rh, sh), h2h);
-  float Q = MCG_FMA(rh, MCG_FMA(rh, MCG_EXP_Q5, MCG_EXP_Q4), MCG_EXP_Q3);
-  float tail = MCG_ADD(MCG_ADD(MCG_MUL(0.5f, q2l), rl), MCG_FMA(rh, rl, MCG_MUL(MCG_MUL(q2h, rh), Q)));
-  sl = MCG_ADD(sl, tail);
-  int j = k & 63;
+  const float rh0 = MCG_SUB(r1, p2);
+  const float bv = MCG_SUB(rh0, r1);
+  const float re = MCG_SUB(MCG_SUB(r1, MCG_SUB(rh0, bv)), MCG_ADD(p2, bv));
+  const float rl0 = MCG_SUB(MCG_SUB(re, p2e), MCG_MUL(kf, MCG_EXP_C3));
+  const float rh = MCG_ADD(rh0, rl0);
+  const float rl = MCG_ADD(MCG_SUB(rh0, rh), rl0);
+  float el;
+  const float eh = mcg_exp_small_form(rh, rl, &el); /* e^r = eh + el */
+  const int j = k & 63;
   int q = (k - j) / 64; /* exact floor division: k - j is a multiple of 64 */
-  float thi = T->exp_thi[j];
-  float tlo = T->exp_tlo[j];
-  /* T*(1 + sh + sl) = thi + thi*sh + (thi*sl + tlo + tlo*sh) */
-  float P = MCG_MUL(thi, sh);
-  float Pe = MCG_FMA(thi, sh, -P);
-  float z = MCG_ADD(thi, P);
-  float ze = MCG_ADD(MCG_SUB(thi, z), P);
-  float lo = MCG_ADD(MCG_ADD(ze, Pe), MCG_FMA(thi, sl, MCG_FMA(tlo, sh, tlo)));
-  float yh = MCG_ADD(z, lo);
-  float yl = MCG_ADD(MCG_SUB(z, yh), lo);
-  *delta = mcg_midpoint_delta(yh, yl);
+  const float thi = T->exp_thi[j];
+  const float tlo = T->exp_tlo[j];
+  /* (thi + tlo)(eh + el) = P + (Pe + thi el + tlo eh), renormalised */
+  const float P = MCG_MUL(thi, eh);
+  const float Pe = MCG_FMA(thi, eh, -P);
+  const float lo = MCG_ADD(Pe, MCG_FMA(thi, el, MCG_MUL(tlo, eh)));
+  float yh = MCG_ADD(P, lo);
+  const float yl = MCG_ADD(MCG_SUB(P, yh), lo);
+  *delta = k == 0 ? mcg_exp_small_delta(yl) : mcg_midpoint_delta(yh, yl);
   /* scale by 2^q, q in [-26, 128]; the product is exact unless it overflows */
   if (q > 127) { yh = MCG_MUL(yh, 2.0f); q -= 1; }
   return MCG_MUL(yh, mcg_u2f((uint32_t)(q + 127) << 23));
+}
+
+/* exp(t) for -17.5 <= t < 89 (other arguments give meaningless values,
+ * and touch nothing outside T).  The path is chosen by the argument; in
+ * translation units that define MCG_EXP_UNIFORM a warp whose lanes mix the
+ * two takes the general path for all (identical bits, no divergence). */
+MCG_HD float mcg_exp_ff_core(float t, float *delta, const mcg_libm_tab *T)
+{
+  const int k = mcg_rint_k(MCG_MUL(t, MCG_EXP_INV));
+#if defined(__CUDA_ARCH__) && defined(MCG_EXP_UNIFORM)
+  if (__all_sync(__activemask(), k == 0))
+#else
+  if (k == 0)
+#endif
+    return mcg_exp_ff_small(t, delta);
+  return mcg_exp_ff_general(t, k, delta, T);
 }
 
 /* exp(t) for -17.5 <= t < 89.  Larger t returns +inf with delta 0.5. */

@@ -61,7 +61,7 @@ int main(int argc, char **argv)
   }
   const int nt = omp_get_max_threads();
   std::vector<std::vector<Exc>> log_exc(nt), exp_exc(nt);
-  long long bad_low = 0, bad_high = 0;
+  long long bad_low = 0, bad_high = 0, bad_path = 0;
 
   /* ---- logf on (0, 1] ---- */
   const uint32_t log_hi = 0x3f800000u;
@@ -76,7 +76,7 @@ int main(int argc, char **argv)
   }
 
   /* ---- expf: all floats; [-17.5, 89) tabulated, the rest verified ---- */
-#pragma omp parallel for schedule(dynamic, 1 << 16) reduction(+ : bad_low, bad_high)
+#pragma omp parallel for schedule(dynamic, 1 << 16) reduction(+ : bad_low, bad_high, bad_path)
   for (long long ui = 0; ui <= 0xffffffffll; ++ui) {
     float t = asf((uint32_t)ui);
     if (std::isnan(t))
@@ -97,6 +97,19 @@ int main(int argc, char **argv)
     float y = mcg_exp_ff(t, &d, &kTab);
     if (asu(y) != asu(g))
       exp_exc[omp_get_thread_num()].push_back({(uint32_t)ui, asu(g), d});
+    /* the general path must reproduce the small-argument path (value and
+     * midpoint measure) wherever the latter applies */
+    if (mcg_rint_k(MCG_MUL(t, MCG_EXP_INV)) == 0) {
+      float d2;
+      float y2 = mcg_exp_ff_general(t, 0, &d2, &kTab);
+      if (asu(y2) != asu(y) || asu(d2) != asu(d))
+        bad_path++;
+    }
+  }
+  if (bad_path) {
+    fprintf(stderr, "libm_tablegen: the general exp path differs from the small-argument "
+                    "path on %lld arguments\n", bad_path);
+    return 1;
   }
   if (bad_low || bad_high) {
     fprintf(stderr, "libm_tablegen: host expf violates the tracker's assumptions "

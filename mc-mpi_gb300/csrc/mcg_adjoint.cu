@@ -30,6 +30,12 @@
 #include <cstring>
 #include <vector>
 
+/* A warp whose lanes need both exp paths takes the general one for all: it
+ * returns the small-argument path's bits wherever that applies.  Measured on
+ * the adjoint kernels: about 0.5-1 % faster; on the single-chain tracker, whose
+ * crossings almost all take the small path, 3 % slower, so it keeps the
+ * per-lane choice. */
+#define MCG_EXP_UNIFORM
 #include "mcg_internal.h"
 #include "mcg_track.cuh"
 

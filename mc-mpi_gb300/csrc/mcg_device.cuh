@@ -209,6 +209,20 @@ __device__ __forceinline__ float mcg_one_minus_expf_strict(float t, const mcg_li
   return __fsub_rn(1.0f, y);
 }
 
+/* The exception lookup of expf: y, d from mcg_exp_ff (either path). */
+__device__ __forceinline__ float mcg_exp_fixup(float t, float y, float d, const mcg_libm_dev &L)
+{
+  if (d <= L.tau_exp_max) {
+    uint32_t key = __float_as_uint(t);
+    if (d <= __ldg(L.tau_exp + (key >> 19))) {
+      uint32_t v;
+      if (mcg_hash_find(L.hash_exp, L.mask_exp, L.probes_exp, key, v))
+        y = __uint_as_float(v);
+    }
+  }
+  return y;
+}
+
 __device__ __forceinline__ float mcg_expf_strict(float t, const mcg_libm_tab *T,
                                                  const mcg_libm_dev &L)
 {

@@ -31,7 +31,15 @@ __global__ void mcg_libm_eval_kernel(int fn, const float *in, float *out, int64_
       r = (v >= 0.0f && v <= 1.0f) ? mcg_logf_strict(v, &T, L) : __int_as_float(0x7fc00000);
     else if (fn == 2)
       r = mcg_ex2_approx(v);
-    else
+    else if (fn == 3) {
+      /* expf with the general path forced for every argument */
+      float d = 0.5f;
+      r = __int_as_float(0x7fc00000);
+      if (v >= MCG_EXP_ONE_BOUND && v < 89.0f) {
+        float y = mcg_exp_ff_general(v, mcg_rint_k(__fmul_rn(v, MCG_EXP_INV)), &d, &T);
+        r = mcg_exp_fixup(v, y, d, L);
+      }
+    } else
       r = (v >= MCG_EXP_ONE_BOUND && v < 89.0f) ? mcg_expf_strict(v, &T, L)
                                                 : __int_as_float(0x7fc00000);
     out[i] = r;
@@ -56,7 +64,7 @@ extern "C" int mcg_rnd_real_device(mcg_context *ctx, uint64_t *d_seeds, float *d
 extern "C" int mcg_libm_eval_device(mcg_context *ctx, int fn, const float *d_in, float *d_out,
                                     int64_t n)
 {
-  if (!ctx || fn < 0 || fn > 2 || n < 0 || (n > 0 && (!d_in || !d_out)))
+  if (!ctx || fn < 0 || fn > 3 || n < 0 || (n > 0 && (!d_in || !d_out)))
     return mcg_fail(MCG_ERR_ARG, "mcg_libm_eval_device: bad arguments");
   if (!ctx->libm_loaded)
     return mcg_fail(MCG_ERR_STATE, "mcg_libm_eval_device: needs a strict context");
