@@ -145,10 +145,17 @@ def cpu_rate(n_hist, threads, first=0):
     return n_hist / dt, steps, dt
 
 
-def cpu_baseline(budget_s=12.0, threads=None):
+def cpu_calibrate(threads):
+    """Histories/s of the port on a sample large enough to keep every thread
+    busy (512 histories per thread), used to size the timed samples."""
+    rate, _, _ = cpu_rate(threads * 512, threads, first=1_000_000)
+    return rate
+
+
+def cpu_baseline(budget_s=10.0, threads=None):
     threads = threads or os.cpu_count()
-    rate, steps, dt = cpu_rate(max(threads * 4, 64), threads)
-    n = int(max(threads * 8, min(2_000_000, rate * budget_s)))
+    rate = cpu_calibrate(threads)
+    n = int(max(threads * 8, min(4_000_000, rate * budget_s)))
     rate, steps, dt = cpu_rate(n, threads, first=7_000_000)
     return {"value": rate, "unit": "histories/s", "cores": threads, "kind": "port",
             "sample": f"{n} histories of the 1e8-history source (indices 7e6..), {steps} steps, "
@@ -161,7 +168,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     threads = os.cpu_count()
-    rate, steps, dt = cpu_rate(max(threads * 4, 64), threads)
+    rate = cpu_calibrate(threads)
     per_step = int(max(threads * 8, min(2_000_000, rate * 4.0)))
     times = []
     for k in range(args.warmup + args.steps):

@@ -41,7 +41,8 @@ MCMPIOptions options_from_config(std::string filepath, int world_size)
       fprintf(stderr, "Yaml File %s was not correctly formatted.\n", filepath.c_str());
       exit(1);
     }
-    v[line.substr(0, n)] = line.substr(n + 1);
+    /* the first line with a key wins (src/yaml_loader.cpp:27 emplaces) */
+    v.emplace(line.substr(0, n), line.substr(n + 1));
   }
   auto get = [&](const char *k) -> std::string {
     auto it = v.find(k);
