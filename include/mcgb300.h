@@ -334,7 +334,8 @@ int mcg_rnd_real_device(mcg_context *ctx, uint64_t *d_seeds, float *d_reals, int
 /* Strict-mode libm on the GPU for n arguments (testing aid): fn 0 logf on
  * [0, 1], fn 1 expf on [-17.5, 89) (other arguments give NaN); fn 2 the
  * hardware 2^x of the strict tracker's certain-crossing test; fn 3 expf
- * like fn 1 but through the evaluator's general path for every argument. */
+ * like fn 1 but through the evaluator's general path for every argument;
+ * fn 4 the hardware log2, fn 5 the fast arithmetic's flight log2. */
 int mcg_libm_eval_device(mcg_context *ctx, int fn, const float *d_in, float *d_out, int64_t n);
 
 /* Check of the strict tracker's division by a cached reciprocal against the

@@ -119,7 +119,7 @@ out.append(f"#define MCG_EXP_C1 {fl(float(c1))}")
 out.append(f"#define MCG_EXP_C2 {fl(c2)}")
 out.append(f"#define MCG_EXP_C3 {fl(c3)}")
 out.append(f"#define MCG_EXP_INV {fl(f32(64 / ln2))}")
-for n, name in [(3, "Q3"), (4, "Q4"), (5, "Q5")]:
+for n, name in [(3, "Q3"), (4, "Q4")]:
     out.append(f"#define MCG_EXP_{name} {fl(f32(1 / mpmath.factorial(n)))}")
 # one initializer for the mcg_libm_tab struct of exact_libm.h
 out.append("#define MCG_LIBM_TAB_INIT { \\")

@@ -245,6 +245,21 @@ __device__ __forceinline__ float mcg_expf_strict(float t, const mcg_libm_tab *T,
   return y;
 }
 
+/* log2(h) of the fast arithmetic's flight sample h in (0, 1).  The hardware
+ * log2 is documented to an absolute error of 2^-22 on [0.5, 2]; near 1,
+ * where -log h is as small as a thin cell's collision probability (~1e-4 on
+ * a 10,000-cell slab), that is a relative error of a few 1e-4 in the flight
+ * test.  For u = 1 - h < 2^-8 (u exact) the series -ln(1 - u) = u (1 + u/2 +
+ * u^2/3) (truncation below 2^-26 relative) is used instead. */
+__device__ __forceinline__ float mcg_log2_flight(float h)
+{
+  const float u = __fsub_rn(1.0f, h);
+  float p = fmaf(u, MCG_LOG2E_F * (1.0f / 3.0f), MCG_LOG2E_F * 0.5f);
+  p = fmaf(u, p, MCG_LOG2E_F);
+  const float near1 = -u * p;
+  return u < 0x1p-8f ? near1 : __log2f(h);
+}
+
 /* Fast build: 1 - e^t for t <= 0 to a few ulp without cancellation. */
 __device__ __forceinline__ float mcg_one_minus_exp_fast(float t)
 {

@@ -31,6 +31,10 @@ __global__ void mcg_libm_eval_kernel(int fn, const float *in, float *out, int64_
       r = (v >= 0.0f && v <= 1.0f) ? mcg_logf_strict(v, &T, L) : __int_as_float(0x7fc00000);
     else if (fn == 2)
       r = mcg_ex2_approx(v);
+    else if (fn == 4)
+      r = __log2f(v);
+    else if (fn == 5)
+      r = mcg_log2_flight(v);
     else if (fn == 3) {
       /* expf with the general path forced for every argument */
       float d = 0.5f;
@@ -64,7 +68,7 @@ extern "C" int mcg_rnd_real_device(mcg_context *ctx, uint64_t *d_seeds, float *d
 extern "C" int mcg_libm_eval_device(mcg_context *ctx, int fn, const float *d_in, float *d_out,
                                     int64_t n)
 {
-  if (!ctx || fn < 0 || fn > 3 || n < 0 || (n > 0 && (!d_in || !d_out)))
+  if (!ctx || fn < 0 || fn > 5 || n < 0 || (n > 0 && (!d_in || !d_out)))
     return mcg_fail(MCG_ERR_ARG, "mcg_libm_eval_device: bad arguments");
   if (!ctx->libm_loaded)
     return mcg_fail(MCG_ERR_STATE, "mcg_libm_eval_device: needs a strict context");

@@ -193,7 +193,7 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
   } else {
     const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
     const float om_cross = mcg_one_minus_exp_fast(-sig_a * de);
-    const float di = c.y != 0.0f ? __log2f(h) * c.y : MCG_MAXREAL;
+    const float di = c.y != 0.0f ? mcg_log2_flight(h) * c.y : MCG_MAXREAL;
     const bool coll = di < de;
     if (l_out) {
       *l_out = coll ? di : de;
@@ -282,7 +282,7 @@ __device__ __forceinline__ bool mcg_step_cross(uint64_t &seed, float &x, float &
     }
   } else {
     const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
-    const float di = c.y != 0.0f ? __log2f(h) * c.y : MCG_MAXREAL;
+    const float di = c.y != 0.0f ? mcg_log2_flight(h) * c.y : MCG_MAXREAL;
     if (di < de)
       return false;
     if (l_out) {
@@ -365,7 +365,7 @@ __device__ __forceinline__ void mcg_step_rest(float h, uint64_t &seed, float &x,
   } else {
     const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
     const float om_cross = mcg_one_minus_exp_fast(-sig_a * de);
-    const float di = c.y != 0.0f ? __log2f(h) * c.y : MCG_MAXREAL;
+    const float di = c.y != 0.0f ? mcg_log2_flight(h) * c.y : MCG_MAXREAL;
     const bool coll = di < de;
     if (l_out) {
       *l_out = coll ? di : de;
