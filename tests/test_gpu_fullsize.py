@@ -108,15 +108,19 @@ def test_fullsize_sampled_histories_bit_exact(mcg, oracle, slab):
         assert np.array_equal(ctx.tally_q(), ref["tally_q"])
 
 
-def test_fullsize_fast_accounting_and_additivity(mcg, slab):
+def test_fullsize_fast_accounting_and_additivity(mcg, slab, strict_runs):
     """The fast arithmetic on the same 1e8 histories: exact additivity over
-    two shards, every history ending once, and the born weight conserved to
-    1e-6.  (Its statistical parity with the FP64 oracle is checked at 2e4
-    histories in test_gpu_fast.py; cell by cell against the strict run at
-    1e8 it is not expected: the two draw h on different grids, 2^-23 and
-    2^-24 near 1, which on this slab's thin cells moves each cell's
-    collision probability by a few 1e-4, about one 1e8-history standard
-    error.)"""
+    two shards, every history ending once, the born weight conserved to
+    1e-6, and no drift against the strict run: the mean relative difference
+    over each of three regions of the slab below 3e-5 and over the whole
+    slab below 1e-5.  (Cell by cell the two are not expected to agree to a
+    1e8-history standard error: they draw h on different grids, 2^-23 and
+    2^-24 near 1, which on this slab's thin cells shifts each cell's
+    collision probability by a few 1e-4 either way; their statistical
+    parity with the FP64 oracle is checked at 2e4 histories in
+    test_gpu_fast.py.  A biased flight log near h = 1, or a uniform
+    truncated instead of centred, shows here as a drift of 5e-5 and more.)"""
+    strict = strict_runs[0].astype(np.float64)
     with _context(mcg, slab, "fast") as ctx:
         ctx.simulate_source(0, N, seed_mode=0, base_seed=BASE)
         full_q, c = ctx.tally_q(), ctx.counters()
@@ -130,3 +134,8 @@ def test_fullsize_fast_accounting_and_additivity(mcg, slab):
     assert c["leaked_left"] + c["leaked_right"] + c["killed"] == N
     total = (int(full_q.sum()) + c["w_left_q"] + c["w_right_q"] + c["w_killed_q"]) * 2.0 ** -SCALE
     assert abs(total - N) <= 1e-6 * N
+    fast = full_q.astype(np.float64)
+    rel = (fast - strict) / strict
+    for lo, hi in ((0, 1000), (1000, 5000), (5000, 10000)):
+        assert abs(rel[lo:hi].mean()) < 3e-5, (lo, hi, rel[lo:hi].mean())
+    assert abs(fast.sum() - strict.sum()) < 1e-5 * strict.sum()
