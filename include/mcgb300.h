@@ -318,9 +318,10 @@ int mcg_fit_release(mcg_context *ctx);
  * up that array's device address (cudaGetSymbolAddress) with the current
  * device; make that first call before any stream capture.  The array is
  * shared by all calls on a device and keeps the last call's contents; each
- * call clears what must start at zero.  Calls that overlap on the GPU race
- * on it: serialise them.  Runs on the legacy default stream of the current
- * device and returns when done. */
+ * call clears what must start at zero.  Calls from several host threads of
+ * one process are serialised by a lock inside the library; another process
+ * on the same GPU has its own array.  Runs on the legacy default stream of
+ * the current device and returns when done. */
 #define MCG_NOALLOC_MAX_CELLS 16384
 int mcg_simulate_fast_noalloc(int n_layers, const int32_t *h_index_start, const int32_t *h_m,
                               const float *h_dx, const float *h_sigs, const float *h_rates,

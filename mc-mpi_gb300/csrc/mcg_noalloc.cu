@@ -13,9 +13,11 @@
  * file-scope device array of fixed size, compiled into the library.
  *
  * The array is shared by every call on a device and keeps the previous
- * call's contents; each call clears the parts that must start at zero.
- * Calls that overlap on the GPU (from several host threads or streams) race
- * on it and give wrong results: serialise them.
+ * call's contents; each call clears the parts that must start at zero.  The
+ * call is synchronous and holds a process-wide lock from the scratch set-up
+ * to its return, so calls from several host threads of this process run one
+ * after another; another process on the same GPU has its own copy of the
+ * array.
  */
 #include <cuda_runtime.h>
 
@@ -40,6 +42,8 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[MCG_NOALLOC_BYT
  * device memory. */
 static std::mutex g_noalloc_mu;
 static std::vector<unsigned char *> g_noalloc_addr;
+/* Serialises whole calls (the scratch array is shared). */
+static std::mutex g_noalloc_call_mu;
 
 static int noalloc_scratch(int device, unsigned char **out)
 {
@@ -77,6 +81,7 @@ extern "C" int mcg_simulate_fast_noalloc(int n_layers, const int32_t *h_index_st
     return mcg_fail(MCG_ERR_ARG,
                     "mcg_simulate_fast_noalloc: chain of %d cells exceeds the fixed scratch "
                     "(at most %d cells)", total, MCG_NOALLOC_MAX_CELLS);
+  std::lock_guard<std::mutex> call_lock(g_noalloc_call_mu);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess)
