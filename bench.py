@@ -335,8 +335,9 @@ def run_gpu(args):
     if rank == 0 and not args.no_extra and args.algorithm == "history":
         line["event"] = bench_event(mcg, args.mode, local, st, m, dx, sigs, rates)
     if rank == 0 and not args.no_extra and args.mode == "strict":
-        # the same steps with fast arithmetic (hardware log2/exp2; tallies
-        # statistically equivalent, not bit-identical)
+        # the same steps with fast arithmetic (hardware log2/exp2, a series
+        # for the flight's log near h = 1; tallies statistically equivalent,
+        # not bit-identical)
         fctx = mcg.Context(mode="fast", device=local)
         fctx.set_layers(st, m, dx, sigs, rates, MIN_W)
         fctx.set_tally_scale(35)
