@@ -395,7 +395,11 @@ def bench_batched(mcg, mode, device, scale=0.02, reps=2):
             "speedup_vs_per_slab": (ms_plain / 1e3) / t, "identical_tallies": same,
             "steps_per_s": steps / t, "histories": n, "launches": 1,
             "workload": f"4096 slabs, cells U{{16..4096}}, L~U[0.5,5], sigma_a~U[0.1,5], "
-                        f"sigma_s~U[0,10], histories log-uniform [1e3,1e6] x {scale}"}
+                        f"sigma_s~U[0,10], histories log-uniform [1e3,1e6] x {scale}",
+            "note": None if scale >= 1.0 else
+                    "reduced histories: each per-slab launch is then mostly its fixed cost "
+                    "(set-up and the tail of its longest histories), which inflates the "
+                    "speed-up; bench.py --workload batch measures the full configuration"}
 
 
 def figure_of_merit(ctx, hist_per_s, n_batches=20, size=100_000):
