@@ -60,6 +60,26 @@ def peaks():
         return 6800.0, "fallback"
 
 
+# Rate of the 64-bit int<->float conversions (u64->f32, f32->s64) on a GB300:
+# a micro-benchmark with CUDA events (four independent conversion chains per
+# thread, 1216 x 256 threads) measured 5.97e11/s for each, against 1.07e13/s
+# for u32->f32.  The strict tracker needs two per step (the uniform and the
+# fixed-point deposit) and one more per scatter (the new direction); the
+# fast one only the deposit's.
+CONV64_PER_S = 5.97e11
+
+
+def conversion_roofline(steps, scatters, seconds, mode):
+    """The strict tracker's binding roof: 64-bit conversions per second
+    against the measured rate of that pipe."""
+    per = (2 * steps + scatters) if mode == "strict" else steps
+    achieved = per / seconds
+    return {"bound": "64-bit int/float conversion rate", "achieved": achieved,
+            "peak": CONV64_PER_S, "unit": "conversions/s", "frac": achieved / CONV64_PER_S,
+            "peak_source": "micro-benchmark of the conversion instructions on a GB300 "
+                           "(CUDA events), not re-measured by this run"}
+
+
 def physics(nb=NB_CELLS):
     xc = (np.arange(nb, dtype=np.float64) + 0.5) / nb
     sa = (0.5 + 0.4 * np.sin(6 * np.pi * xc)).astype(np.float32)
@@ -325,6 +345,8 @@ def run_gpu(args):
                      "traffic_unit": "bytes per launch (ncu capture of 3e6 histories, scaled)",
                      "peak_source": peak_kind,
                      "note": "the tracker is issue-bound; see issue_roofline"},
+        "conversion_roofline": conversion_roofline(counters["steps"] * ws,
+                                                   counters["scatters"] * ws, dev_s, args.mode),
         "issue_roofline": {"bound": "issue", "n_alg_ops_per_step": n_alg,
                            "achieved_gops": (counters["steps"] / dev_s) * n_alg / 1e9,
                            "peak_gops": sms * 128 * f_sm / 1e9, "frac": issue_frac},

@@ -40,3 +40,11 @@ def test_reference_arm_prints_the_contract_line(oracle):
 
 def test_reference_arm_other_ranks_exit_quietly():
     assert _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []
+
+
+def test_conversion_roofline_arithmetic():
+    import bench
+    r = bench.conversion_roofline(10, 2, 1e-10, "strict")
+    assert r["achieved"] == 22 / 1e-10 and r["peak"] == bench.CONV64_PER_S
+    assert abs(r["frac"] - 22 / 1e-10 / bench.CONV64_PER_S) < 1e-12
+    assert bench.conversion_roofline(10, 2, 1.0, "fast")["achieved"] == 10
