@@ -344,7 +344,9 @@ def run_gpu(args):
                      "traffic": dram_per_hist * B if args.mode == "strict" else None,
                      "traffic_unit": "bytes per launch (ncu capture of 3e6 histories, scaled)",
                      "peak_source": peak_kind,
-                     "note": "the tracker is issue-bound; see issue_roofline"},
+                     "note": "not HBM-bound: the 64-bit conversion rate and instruction "
+                             "issue bound the tracker; see conversion_roofline and "
+                             "issue_roofline"},
         "conversion_roofline": conversion_roofline(counters["steps"] * ws,
                                                    counters["scatters"] * ws, dev_s, args.mode),
         "issue_roofline": {"bound": "issue", "n_alg_ops_per_step": n_alg,
