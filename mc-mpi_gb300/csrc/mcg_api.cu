@@ -125,20 +125,23 @@ int mcg_load_libm(mcg_context *ctx)
   ctx->libm.tau_log_max = tl;
   ctx->libm.tau_exp_max = te;
   cudaError_t e;
-  float *dtl, *dte;
-  uint2 *dhl, *dhe;
-  mcg_libm_tab *dtab;
-  if ((e = cudaMalloc(&dtl, sizeof(hdr.tau_log))) != cudaSuccess ||
-      (e = cudaMalloc(&dte, sizeof(hdr.tau_exp))) != cudaSuccess ||
-      (e = cudaMalloc(&dhl, hl.size() * sizeof(uint2))) != cudaSuccess ||
-      (e = cudaMalloc(&dhe, he.size() * sizeof(uint2))) != cudaSuccess ||
-      (e = cudaMalloc(&dtab, sizeof(tab))) != cudaSuccess)
+  float *dtl = nullptr, *dte = nullptr;
+  uint2 *dhl = nullptr, *dhe = nullptr;
+  mcg_libm_tab *dtab = nullptr;
+  /* each allocation joins the context's list as soon as it exists, so a
+   * failure part-way leaves nothing behind at mcg_destroy */
+  auto alloc = [ctx](void **p, size_t bytes) {
+    cudaError_t r = cudaMalloc(p, bytes);
+    if (r == cudaSuccess)
+      ctx->owned.push_back(*p);
+    return r;
+  };
+  if ((e = alloc((void **)&dtl, sizeof(hdr.tau_log))) != cudaSuccess ||
+      (e = alloc((void **)&dte, sizeof(hdr.tau_exp))) != cudaSuccess ||
+      (e = alloc((void **)&dhl, hl.size() * sizeof(uint2))) != cudaSuccess ||
+      (e = alloc((void **)&dhe, he.size() * sizeof(uint2))) != cudaSuccess ||
+      (e = alloc((void **)&dtab, sizeof(tab))) != cudaSuccess)
     return mcg_cuda_fail(e, "cudaMalloc(libm tables)");
-  ctx->owned.push_back(dtl);
-  ctx->owned.push_back(dte);
-  ctx->owned.push_back(dhl);
-  ctx->owned.push_back(dhe);
-  ctx->owned.push_back(dtab);
   if ((e = cudaMemcpy(dtl, hdr.tau_log, sizeof(hdr.tau_log), cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(dte, hdr.tau_exp, sizeof(hdr.tau_exp), cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(dhl, hl.data(), hl.size() * sizeof(uint2), cudaMemcpyHostToDevice)) != cudaSuccess ||
@@ -194,14 +197,15 @@ extern "C" int mcg_create(int device, int mode, mcg_context **out)
                        (e = cudaEventCreate(&ctx->ev1)) != cudaSuccess))
     rc = mcg_cuda_fail(e, "stream/event create");
   if (rc == MCG_OK) {
-    if ((e = cudaMalloc(&ctx->d_counters, 16 * sizeof(unsigned long long))) != cudaSuccess ||
-        (e = cudaMalloc(&ctx->d_next, 8 * sizeof(unsigned long long))) != cudaSuccess)
-      rc = mcg_cuda_fail(e, "cudaMalloc(counters)");
-    else {
+    if ((e = cudaMalloc(&ctx->d_counters, 16 * sizeof(unsigned long long))) == cudaSuccess)
       ctx->owned.push_back(ctx->d_counters);
+    if (e == cudaSuccess &&
+        (e = cudaMalloc(&ctx->d_next, 8 * sizeof(unsigned long long))) == cudaSuccess)
       ctx->owned.push_back(ctx->d_next);
+    if (e != cudaSuccess)
+      rc = mcg_cuda_fail(e, "cudaMalloc(counters)");
+    else
       cudaMemset(ctx->d_counters, 0, 16 * sizeof(unsigned long long));
-    }
   }
   if (rc == MCG_OK && mode == MCG_MODE_STRICT)
     rc = mcg_load_libm(ctx);
