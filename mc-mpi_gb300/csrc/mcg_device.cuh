@@ -49,10 +49,11 @@ __device__ __forceinline__ float mcg_u63_unit(uint64_t s)
 }
 
 /* rnd_real: s <- (G s + C) mod 2^63; h = RN((float)s) * 2^-63.
- * The hardware conversion issues on the FP64 pipe, which the tracker
- * otherwise leaves idle while its integer/logic pipe is the busiest (measured
- * +31 % steps/s over mcg_u63_unit); MCG_INT_CONVERSIONS selects the integer
- * version (same bits). */
+ * The hardware conversion issues on the FP64 pipe (about 6e11 64-bit
+ * conversions/s per GB300); with this one and the deposit's per step it is
+ * the strict tracker's tightest resource, yet the integer version
+ * (MCG_INT_CONVERSIONS, same bits) costs more issue slots than it frees
+ * (measured +31 % steps/s for the hardware form when it was introduced). */
 __device__ __forceinline__ float mcg_rnd_real(uint64_t &s)
 {
   s = (MCG_RNG_G * s + MCG_RNG_C) & MCG_MASK63;
