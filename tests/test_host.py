@@ -87,3 +87,18 @@ def test_config_loader_errors(config_exe, tmp_path):
     r = subprocess.run([config_exe, str(tmp_path / "missing.yaml"), "1"], capture_output=True,
                        text=True)
     assert r.returncode != 0 and "Couldn't open" in r.stderr
+
+
+@pytest.mark.parametrize("name", sorted(f[:-4] for f in os.listdir(os.path.join(ROOT, "tests", "cpp"))
+                                        if f.endswith(".cpp")))
+def test_cpp_programs_build_against_the_api(built, tmp_path, name):
+    """Every C++ test program (the GPU ones included) compiles and links
+    against the installed headers and libmcgb300.so: the C++ API the
+    reference's callers use stays in step with the library."""
+    libdir = os.path.dirname(built.LIB)
+    r = subprocess.run(["g++", "-O0", "-std=c++17", "-I" + os.path.join(ROOT, "include"),
+                        "-I" + os.path.join(PKG_DIR, "host", "include"),
+                        os.path.join(ROOT, "tests", "cpp", name + ".cpp"), "-L" + libdir,
+                        "-lmcgb300", "-Wl,-rpath," + libdir, "-o", str(tmp_path / name)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
