@@ -13,8 +13,13 @@ launch, so the launch's tail, where the SMs wait on the longest histories,
 is paid once per 1e8).  Synthetic data: the reference has no dataset.
 
 batched / adjoint : the metric's other two forms (batched slabs of
-        configuration 2, forward+adjoint of configuration 3), each timed with
-        CUDA events on its own launch.
+        configuration 2 at full size, autotuned, against one launch per slab;
+        forward+adjoint of configuration 3), each timed with CUDA events on
+        its own launch.
+worker : the workers' cycle with on-device hand-over queues on the first
+        1e7 histories, against the fused tracker (identical tallies).
+fit   : configuration 4, the batched inverse fit (200 Adam steps of batched
+        forward+adjoint launches replayed from a CUDA graph).
 value : histories/s of the strict tracker with the batch's particles
         already resident in HBM (mcg_simulate_device), CUDA-event time of
         the kernel, L2 flushed (256 MB memset) between steps.
@@ -46,6 +51,9 @@ METRIC = "histories/s on 1 GB300 (plain vs batched vs fwd+adjoint) at matched ta
 NB_CELLS, N_LAYERS, N_TOTAL = 10000, 64, 100_000_000
 BASE_SEED = 5127801
 MIN_W = 1e-12
+# DRAM bytes (read + write) per history of the strict tracker, from an ncu
+# capture of 3e6 histories of this workload
+DRAM_BYTES_PER_HISTORY = 112.44e6 / 3e6
 WORKLOAD = ("slab 10000 cells / 64 sub-domains (decompose_domain), sigma_a=0.5+0.4sin(6pi x), "
             "sigma_s=2+1.5cos(4pi x), 1e8 histories from x=0 mu=1 w=1, rnd_seed chain 5127801, "
             "min weight 1e-12")
@@ -60,24 +68,23 @@ def peaks():
         return 6800.0, "fallback"
 
 
-# Rate of the 64-bit int<->float conversions (u64->f32, f32->s64) on a GB300:
-# a micro-benchmark with CUDA events (four independent conversion chains per
-# thread, 1216 x 256 threads) measured 5.97e11/s for each, against 1.07e13/s
-# for u32->f32.  The strict tracker needs two per step (the uniform and the
-# fixed-point deposit) and one more per scatter (the new direction); the
-# fast one only the deposit's.
-CONV64_PER_S = 5.97e11
-
-
-def conversion_roofline(steps, scatters, seconds, mode):
-    """The strict tracker's binding roof: 64-bit conversions per second
-    against the measured rate of that pipe."""
-    per = (2 * steps + scatters) if mode == "strict" else steps
+def conversion_roofline(steps, scatters, seconds, mode, rates):
+    """64-bit int<->float conversions per second against the rate of that
+    pipe measured in this run (mcg_measure_conversion_rates).  The strict
+    tracker converts a state to a float only where the value itself is
+    needed: the flight sample and the new direction of a scatter (2 per
+    scatter; the certain-crossing test compares the state's top bits as an
+    integer, and deposits below 2^31 fixed-point units take the 32-bit
+    conversion).  The near-ties that also need the flight sample (about 2e-5
+    of the crossings) and the rare deposits of 2^31 units and more are not
+    counted.  The fast tracker uses no 64-bit conversion per step."""
+    per = 2 * scatters if mode == "strict" else 0
+    peak = min(rates["u64_f32"], rates["f32_s64"])
     achieved = per / seconds
-    return {"bound": "64-bit int/float conversion rate", "achieved": achieved,
-            "peak": CONV64_PER_S, "unit": "conversions/s", "frac": achieved / CONV64_PER_S,
-            "peak_source": "micro-benchmark of the conversion instructions on a GB300 "
-                           "(CUDA events), not re-measured by this run"}
+    return {"bound": "64-bit int/float conversion rate (not binding)", "achieved": achieved,
+            "peak": peak, "unit": "conversions/s", "frac": achieved / peak,
+            "peak_source": "measured in this run (mcg_measure_conversion_rates)",
+            "measured_rates": rates}
 
 
 def physics(nb=NB_CELLS):
@@ -307,11 +314,12 @@ def run_gpu(args):
     # roofline of the tracker kernel: algorithmic bytes per launch
     hbm_peak, peak_kind = peaks()
     bytes_per_hist = 24 + 24 + 4  # particle in, particle out, result
-    # DRAM bytes (read + write) per history of one ncu capture of this kernel
-    # (3e6 histories, 112.4 MB; profiles/track_strict_slab10k_ncu.md), scaled
-    # to the launch: below the algorithmic 52 B because part of the particle
-    # write-back is still in L2 when the kernel ends
-    dram_per_hist = 112.44e6 / 3e6
+    # DRAM bytes (read + write) per history from one ncu capture of this
+    # kernel on 3e6 histories of the same workload (a constant of this file,
+    # not measured by this run), scaled to the launch: below the algorithmic
+    # 52 B because part of the particle write-back is still in L2 when the
+    # kernel ends
+    dram_per_hist = DRAM_BYTES_PER_HISTORY
     mean_ms = sum(kernel_ms) / len(kernel_ms)
     achieved = bytes_per_hist * B / (mean_ms / 1e3) / 1e9
     steps_per_s = counters["steps"] / dev_s if not dist else None
@@ -342,13 +350,16 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak,
                      "traffic": dram_per_hist * B if args.mode == "strict" else None,
-                     "traffic_unit": "bytes per launch (ncu capture of 3e6 histories, scaled)",
+                     "traffic_unit": "bytes per launch",
+                     "traffic_source": "constant from an ncu capture of 3e6 histories of this "
+                                       "workload (dram__bytes_read.sum + dram__bytes_write.sum), "
+                                       "scaled by histories; not measured by this run",
                      "peak_source": peak_kind,
-                     "note": "not HBM-bound: the 64-bit conversion rate and instruction "
-                             "issue bound the tracker; see conversion_roofline and "
+                     "note": "not HBM-bound: instruction issue bounds the tracker; see "
                              "issue_roofline"},
         "conversion_roofline": conversion_roofline(counters["steps"] * ws,
-                                                   counters["scatters"] * ws, dev_s, args.mode),
+                                                   counters["scatters"] * ws, dev_s, args.mode,
+                                                   ctx.conversion_rates()),
         "issue_roofline": {"bound": "issue", "n_alg_ops_per_step": n_alg,
                            "achieved_gops": (counters["steps"] / dev_s) * n_alg / 1e9,
                            "peak_gops": sms * 128 * f_sm / 1e9, "frac": issue_frac},
@@ -381,6 +392,27 @@ def run_gpu(args):
     if rank == 0 and not args.no_extra:
         line["batched"] = bench_batched(mcg, args.mode, local)
         line["adjoint"] = bench_adjoint(mcg, args.mode, local)
+        line["worker"] = bench_worker(mcg, args.mode, local, st, m, dx, sigs, rates)
+        line["fit"] = bench_fit(mcg, local)
+    if dist:
+        # exact multi-rank reduction: every rank runs its share of 1e5
+        # histories, the int64 tallies are summed over ranks, and rank 0
+        # compares with one rank running all of them
+        from mc_mpi_gb300 import dist as mdist
+        n_check = 100_000
+
+        def run_shard(first, count):
+            ctx.tally_reset()
+            ctx.simulate_source(N_TOTAL + first, count)
+            return torch.from_numpy(ctx.tally_q())
+
+        red = mdist.sharded_tally(run_shard, n_check, ws, rank, device="cuda")
+        if rank == 0:
+            ctx.tally_reset()
+            ctx.simulate_source(N_TOTAL, n_check)
+            line["multi_rank_check"] = {
+                "histories": n_check, "ranks": ws,
+                "identical_tallies": bool(np.array_equal(red.cpu().numpy(), ctx.tally_q()))}
     if rank == 0 and ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:
@@ -391,17 +423,19 @@ def run_gpu(args):
     return 0
 
 
-def bench_batched(mcg, mode, device, scale=0.02, reps=2):
+def bench_batched(mcg, mode, device, scale=1.0, reps=2):
     """Configuration 2 (4096 slabs, cells U{16..4096}, L ~ U[0.5, 5], per-cell
     sigma_a ~ U[0.1, 5], sigma_s ~ U[0, 10], histories log-uniform in
-    [1e3, 1e6] scaled by `scale`): one persistent CUDA-graph launch against
-    one ordinary launch per slab, same histories, same tallies."""
+    [1e3, 1e6] scaled by `scale`), launch shape and algorithm picked by the
+    autotuner: one persistent CUDA-graph launch against one ordinary launch
+    per slab, same histories, same tallies."""
     from mc_mpi_gb300 import workloads
     slabs, sigs, rates = workloads.config2(scale_histories=scale)
     n = sum(d["n_histories"] for d in slabs)
     with mcg.Context(mode=mode, device=device) as ctx:
-        ctx.set_tally_scale(32)
+        ctx.set_tally_scale(30)
         ctx.batch_set(slabs, sigs, rates, MIN_W)
+        tune = ctx.batch_autotune(0.05)
         ctx.batch_run()  # warm-up, builds the graph
         ms = []
         for _ in range(reps):
@@ -417,13 +451,74 @@ def bench_batched(mcg, mode, device, scale=0.02, reps=2):
     t = min(ms) / 1e3
     return {"value": n / t, "unit": "histories/s", "per_slab_value": n / (ms_plain / 1e3),
             "speedup_vs_per_slab": (ms_plain / 1e3) / t, "identical_tallies": same,
-            "steps_per_s": steps / t, "histories": n, "launches": 1,
+            "steps_per_s": steps / t, "histories": n, "launches": 1, "autotuned": tune,
             "workload": f"4096 slabs, cells U{{16..4096}}, L~U[0.5,5], sigma_a~U[0.1,5], "
                         f"sigma_s~U[0,10], histories log-uniform [1e3,1e6] x {scale}",
             "note": None if scale >= 1.0 else
                     "reduced histories: each per-slab launch is then mostly its fixed cost "
                     "(set-up and the tail of its longest histories), which inflates the "
-                    "speed-up; bench.py --workload batch measures the full configuration"}
+                    "speed-up"}
+
+
+def bench_worker(mcg, mode, device, st, m, dx, sigs, rates, n=10_000_000):
+    """The workers' cycle with on-device hand-over queues (mcg_worker_run,
+    the form that replaces WorkerSync/Async/Rma's MPI exchange) on the first
+    n histories of the workload, against the fused tracker on the same
+    histories (identical tallies expected)."""
+    with mcg.Context(mode=mode, device=device) as ctx:
+        ctx.set_layers(st, m, dx, sigs, rates, MIN_W)
+        ctx.set_tally_scale(35)
+        ctx.simulate_source(0, n // 10)  # warm-up
+        ctx.tally_reset()
+        ctx.simulate_source(0, n)
+        t_fused = ctx.last_kernel_ms() / 1e3
+        q_fused = ctx.tally_q()
+        ctx.tally_reset()
+        ctx.worker_run(n // 10)  # warm-up
+        ctx.tally_reset()
+        cycles, hand = ctx.worker_run(n)
+        t_w = ctx.last_kernel_ms() / 1e3
+        same = bool(np.array_equal(ctx.tally_q(), q_fused))
+    return {"value": n / t_w, "unit": "histories/s", "fused_value": n / t_fused,
+            "ratio_vs_fused": t_fused / t_w, "identical_tallies": same, "cycles": cycles,
+            "handoffs_per_history": hand / n, "histories": n,
+            "workload": "the plain workload's first 1e7 histories, 64 sub-domains with "
+                        "on-device hand-over queues"}
+
+
+def bench_fit(mcg, device, scale=1.0, n_steps=200):
+    """Configuration 4: 64 slabs with cells U{64..1024}, hidden
+    sigma_a = 1 + 0.8 sin(2 pi k x + phi), sigma_s = 1.5; targets from 1e7
+    histories per slab; 200 Adam steps (lr 1e-2) from sigma_a = 1, each a
+    batched forward+adjoint launch of 1e6 histories per slab (fast
+    arithmetic), all replayed from one CUDA graph.  Reports histories/s of
+    the fit and the final relative L2 error of sigma_a."""
+    from mc_mpi_gb300 import workloads
+    slabs, hidden, sig_s = workloads.config4(histories=int(1e6 * scale))
+    tslabs = [dict(d, n_histories=int(1e7 * scale), base_seed=d["base_seed"] + 1)
+              for d in slabs]
+    sigs = (hidden + sig_s).astype(np.float32)
+    rates = (hidden / sigs).astype(np.float32)
+    with mcg.Context(mode="fast", device=device) as ctx:
+        ctx.batch_set(tslabs, sigs, rates, MIN_W)
+        ctx.batch_run()
+        npc = np.concatenate([np.full(d["n_cells"], d["n_histories"]) for d in tslabs])
+        target = ctx.batch_tally() / npc
+        ctx.fit_set(slabs, np.ones_like(hidden), sig_s, target, max_steps=n_steps)
+        ctx.fit_run(n_steps, lr=1e-2)
+        ms = ctx.last_kernel_ms()
+        sig, loss = ctx.fit_read()
+    hist = n_steps * sum(d["n_histories"] for d in slabs)
+    err0 = float(np.linalg.norm(1.0 - hidden) / np.linalg.norm(hidden))
+    err = float(np.linalg.norm(sig - hidden) / np.linalg.norm(hidden))
+    return {"value": hist / (ms / 1e3), "unit": "histories/s", "adam_steps": n_steps,
+            "histories": hist, "ms_per_adam_step": ms / n_steps, "gpu_launches": 3 * n_steps,
+            "rel_l2_error": err, "rel_l2_error_start": err0, "loss_first": float(loss[0]),
+            "loss_last": float(loss[-1]), "mode": "fast",
+            "workload": f"configuration 4: 64 slabs, cells U{{64..1024}}, hidden "
+                        f"sigma_a=1+0.8sin(2pi k x+phi), sigma_s=1.5, {n_steps} Adam steps lr "
+                        f"1e-2, {int(1e6 * scale)} histories per slab and step, targets from "
+                        f"{int(1e7 * scale)} per slab"}
 
 
 def figure_of_merit(ctx, hist_per_s, n_batches=20, size=100_000):
@@ -557,32 +652,23 @@ def run_workload(args):
         base.update(bench_adjoint(mcg, args.mode, 0))
         base["config"] = {"workload": base.pop("workload"), "mode": args.mode}
     elif args.workload == "fit":
-        slabs, hidden, sig_s = workloads.config4(histories=int(1e6 * args.scale))
-        tslabs = [dict(d, n_histories=int(1e7 * args.scale), base_seed=d["base_seed"] + 1)
-                  for d in slabs]
-        sigs = (hidden + sig_s).astype(np.float32)
-        rates = (hidden / sigs).astype(np.float32)
-        n_steps = 200
-        with mcg.Context(mode="fast") as ctx, ClockSampler(0) as clk:
-            ctx.batch_set(tslabs, sigs, rates, MIN_W)
-            ctx.batch_run()
-            npc = np.concatenate([np.full(d["n_cells"], d["n_histories"]) for d in tslabs])
-            target = ctx.batch_tally() / npc
-            ctx.fit_set(slabs, np.ones_like(hidden), sig_s, target, max_steps=n_steps)
-            ctx.fit_run(n_steps, lr=1e-2)
-            ms = ctx.last_kernel_ms()
-            sig, loss = ctx.fit_read()
-        hist = n_steps * sum(d["n_histories"] for d in slabs)
-        err0 = float(np.linalg.norm(1.0 - hidden) / np.linalg.norm(hidden))
-        err = float(np.linalg.norm(sig - hidden) / np.linalg.norm(hidden))
-        base.update(value=hist / (ms / 1e3), ms_per_step=ms / n_steps, gpu_launches=3 * n_steps,
-                    config={"workload": "configuration 4: 64 slabs, cells U{64..1024}, hidden "
-                                        "sigma_a=1+0.8sin(2pi k x+phi), sigma_s=1.5, 200 Adam "
-                                        f"steps lr 1e-2, {int(1e6 * args.scale)} histories per "
-                                        "slab and step, targets from "
-                                        f"{int(1e7 * args.scale)} per slab", "mode": "fast"},
-                    rel_l2_error=err, rel_l2_error_start=err0,
-                    loss_first=float(loss[0]), loss_last=float(loss[-1]), clocks=clk.summary())
+        with ClockSampler(0) as clk:
+            r = bench_fit(mcg, 0, scale=args.scale)
+        base.update(value=r["value"], ms_per_step=r["ms_per_adam_step"],
+                    gpu_launches=r["gpu_launches"],
+                    config={"workload": r["workload"], "mode": "fast"},
+                    rel_l2_error=r["rel_l2_error"], rel_l2_error_start=r["rel_l2_error_start"],
+                    loss_first=r["loss_first"], loss_last=r["loss_last"], clocks=clk.summary())
+    elif args.workload == "worker":
+        sigs, rates = physics()
+        st, m, dx, _, _ = mcg.layer_decomposition(0.0, 1.0, NB_CELLS, N_LAYERS)
+        with ClockSampler(0) as clk:
+            r = bench_worker(mcg, args.mode, 0, st, m, dx, sigs, rates,
+                             n=int(1e7 * args.scale))
+        base.update(value=r["value"], gpu_launches=2 * r["cycles"], clocks=clk.summary(),
+                    config={"workload": r["workload"], "mode": args.mode},
+                    **{k: r[k] for k in ("fused_value", "ratio_vs_fused", "identical_tallies",
+                                         "cycles", "handoffs_per_history")})
     print(json.dumps(base))
     return 0
 
@@ -601,11 +687,12 @@ def main():
     ap.add_argument("--algorithm", default="history", choices=["history", "event"],
                     help="single-chain tracker: history-based (default) or event-based")
     ap.add_argument("--event-steps", type=int, default=4, help="event mode: events per pass")
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "adjoint", "fit"])
+    ap.add_argument("--workload", default="plain",
+                    choices=["plain", "batch", "adjoint", "fit", "worker"])
     ap.add_argument("--scale", type=float, default=1.0,
                     help="fraction of the configuration's histories (batch, fit)")
     ap.add_argument("--no-extra", action="store_true",
-                    help="skip the batched and adjoint measurements")
+                    help="skip the fast, event, batched, adjoint, worker and fit measurements")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -209,6 +209,27 @@ int mcg_cusimulate(int n, mcg_particle *particles, const float *sigs, const floa
 int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n, int32_t per_cycle,
                    int64_t queue_capacity, int64_t *h_cycles, int64_t *h_handoffs);
 
+/* ---- The asynchronous workers: hand-over without cycles ----
+ * Drop-in for WorkerAsync/WorkerRma::spin (src/worker_async.cpp:19-105,
+ * src/worker_rma.cpp) with AsyncComm/RmaComm's send and receive
+ * (src/async_comm.cpp:17-168, src/rma_comm.cpp:133-225) replaced by bounded
+ * on-device rings, one per sub-domain: one persistent launch in which every
+ * warp takes particles from any sub-domain's ring (or newborns from the
+ * source for the sub-domain holding src->cell0), simulates each inside its
+ * sub-domain and appends leavers to the neighbour's ring, until all n
+ * histories are finished.  A ring holding queue_capacity particles when
+ * another arrives makes the call return MCG_ERR_OVERFLOW (the reference
+ * aborts on a full buffer).  A warp takes queued particles before
+ * newborns, so the rings together hold about as many particles as the GPU
+ * has resident threads (SMs x 1024); twice that per ring is ample.  Warps
+ * without work poll with short sleeps and give up with
+ * MCG_ERR_TIMEOUT after 2 s in which no history finished.  Tallies and
+ * counters as the other entry points (equal to the fused tracker's);
+ * *h_handoffs (may be NULL) counts the hand-overs.  The rings are kept in
+ * the context between calls. */
+int mcg_worker_run_async(mcg_context *ctx, const mcg_source *src, int64_t n,
+                         int64_t queue_capacity, int64_t *h_handoffs);
+
 /* ---- Batched slabs: thousands of independent slabs in one launch ----
  * Slab s is a Layer(0, 1, 0, n_cells) (dx = 1/n_cells, both faces leak):
  * a slab [0, L] maps onto it exactly by scaling its cross sections by L
@@ -243,12 +264,18 @@ int mcg_batch_tally_read(mcg_context *ctx, int64_t *h_q, double *h_f64);
  * (as mcg_set_tally_mode). 0 keeps the current value. */
 int mcg_batch_set_launch(mcg_context *ctx, int32_t block, int64_t item_histories,
                          int32_t tally_mode);
+/* Deferral of the full step in mcg_batch_run (0 off, the default; 1 on):
+ * a lane whose step is not a certain crossing stops stepping for the rest
+ * of its refill round, and the warp's stopped lanes complete their steps
+ * together at the round's end, instead of the warp running the full step
+ * once for every step any of its lanes needs it.  Same results. */
+int mcg_batch_set_deferral(mcg_context *ctx, int32_t defer);
 /* Autotuner: times every candidate on a sample of each slab's histories
  * (fraction in (0, 1], raised so that the sample holds at least four times
  * the event engine's drain size, or the whole run): the history-based
- * launch shapes (block, histories per work item, tally privatisation) and
- * the event-based form at 4 and 16 events per pass, and keeps the one with
- * the least time per history.  Reports the choice and its sample time; the
+ * launch shapes (block, histories per work item, tally privatisation,
+ * deferral of the full step) and the event-based form at 4 and 16 events
+ * per pass, and keeps the one with the least time per history.  Reports the choice and its sample time; the
  * batch tally and counters are reset afterwards. */
 typedef struct mcg_batch_tuning {
   int32_t block;
@@ -258,6 +285,7 @@ typedef struct mcg_batch_tuning {
   int32_t candidates;
   int32_t algorithm;      /* MCG_ALGO_HISTORY or MCG_ALGO_EVENT */
   int32_t steps_per_pass; /* event mode: events per pass */
+  int32_t defer;          /* history mode: deferral of the full step (0/1) */
 } mcg_batch_tuning;
 int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_batch_tuning *out);
 
@@ -302,6 +330,13 @@ int mcg_fit_run(mcg_context *ctx, int32_t n_steps, float lr, float beta1, float 
 /* sig_a of every cell, loss of every step so far (max_steps entries), steps done. */
 int mcg_fit_read(mcg_context *ctx, float *h_sig_a, double *h_loss_hist, int32_t *h_steps);
 int mcg_fit_release(mcg_context *ctx);
+/* Testing aid: one forward + adjoint launch of the fit's kernel at the
+ * current sig_a with loss weights h_weights (per cell) instead of
+ * 2 (a - t), on the histories the next step would run; h_tally = weight
+ * absorbed per history, h_grad = dF/dsig_a per history for
+ * F = sum_c w_c a_c (compare mcg_adjoint_read).  Leaves the fit's state as
+ * it was. */
+int mcg_fit_gradient(mcg_context *ctx, const double *h_weights, double *h_tally, double *h_grad);
 
 /* Fast tracker that allocates no device memory (no counterpart in the
  * reference; this library's addition for callers that may not call
@@ -310,24 +345,43 @@ int mcg_fit_release(mcg_context *ctx);
  * fast-mode context with mcg_set_layers + mcg_set_tally_scale(log2_scale) +
  * mcg_simulate_device + mcg_tally_read: the caller passes the layers and
  * cross sections (host arrays, as mcg_set_layers), the particles (device,
- * updated in place), an optional device result array and the device output
- * d_tally_q[total cells], which is overwritten with the fixed-point tally.
- * Everything else lives in one statically sized device array inside the
- * library, holding chains of at most MCG_NOALLOC_MAX_CELLS cells (larger
- * chains are rejected with MCG_ERR_ARG).  The first call on a device looks
- * up that array's device address (cudaGetSymbolAddress) with the current
- * device; make that first call before any stream capture.  The array is
- * shared by all calls on a device and keeps the last call's contents; each
- * call clears what must start at zero.  Calls from several host threads of
- * one process are serialised by a lock inside the library; another process
- * on the same GPU has its own array.  Runs on the legacy default stream of
- * the current device and returns when done. */
+ * 8-byte aligned, updated in place), an optional device result array and the
+ * device output d_tally_q[total cells], which is overwritten with the
+ * fixed-point tally.  Everything else lives in one statically sized device
+ * array inside the library (about 384 KiB, held by every GPU that loads the
+ * library until the process exits), which holds chains of at most
+ * MCG_NOALLOC_MAX_CELLS cells (larger chains are rejected with MCG_ERR_ARG
+ * before any device work).  Every call looks up that array's device address
+ * (cudaGetSymbolAddress) on the current device, so a device reset between
+ * calls is harmless.  The array is shared by all calls on a device and keeps
+ * the last call's contents; each call clears what must start at zero.  Calls
+ * from several host threads of one process are serialised by a lock inside
+ * the library; calls that overlap on the GPU from other processes use their
+ * own copies.  Runs on the legacy default stream of the current device and
+ * returns when done, so it must not be called while any stream of the
+ * device is being captured into a CUDA graph. */
 #define MCG_NOALLOC_MAX_CELLS 16384
 int mcg_simulate_fast_noalloc(int n_layers, const int32_t *h_index_start, const int32_t *h_m,
                               const float *h_dx, const float *h_sigs, const float *h_rates,
                               float particle_min_weight, int32_t log2_scale,
                               mcg_particle *d_particles, int64_t n, int32_t *d_results,
                               int64_t *d_tally_q);
+
+/* Throughput of the int <-> float conversions on this GPU (testing aid for
+ * the roofline; no counterpart in the reference), conversions per second:
+ * h_rates[0] u64 -> f32, [1] f32 -> s64 (both on the FP64 pipe of a GB300),
+ * [2] u32 -> f32, [3] f32 -> u32; CUDA events around a launch of four
+ * independent conversion chains per thread on 8 x SMs x 256 threads. */
+int mcg_measure_conversion_rates(mcg_context *ctx, double *h_rates);
+
+/* Testing aid (no counterpart in the reference): the after-th next device
+ * allocation of the geometry set-up (mcg_set_layers, mcg_set_layers_xs,
+ * mcg_set_slab, mcg_batch_set; 0 = the next one) reports
+ * cudaErrorMemoryAllocation without being attempted, so tests can check that
+ * a failed set-up leaves the context with no geometry (later launches and
+ * reads return MCG_ERR_STATE) and that a new set-up recovers it.  A negative
+ * value disables it.  Process-wide. */
+int mcg_testing_fail_allocation(int32_t after);
 
 /* One rnd_real step on n device seeds (src/curandom.cu:7-14). */
 int mcg_rnd_real_device(mcg_context *ctx, uint64_t *d_seeds, float *d_reals, int64_t n);
@@ -336,7 +390,9 @@ int mcg_rnd_real_device(mcg_context *ctx, uint64_t *d_seeds, float *d_reals, int
  * [0, 1], fn 1 expf on [-17.5, 89) (other arguments give NaN); fn 2 the
  * hardware 2^x of the strict tracker's certain-crossing test; fn 3 expf
  * like fn 1 but through the evaluator's general path for every argument;
- * fn 4 the hardware log2, fn 5 the fast arithmetic's flight log2. */
+ * fn 4 the hardware log2, fn 5 the flight log2 of a float sample h,
+ * fn 6 the fast arithmetic's flight log2 of the sample whose state has top
+ * 32 bits t, t passed as the argument's bit pattern. */
 int mcg_libm_eval_device(mcg_context *ctx, int fn, const float *d_in, float *d_out, int64_t n);
 
 /* Check of the strict tracker's division by a cached reciprocal against the

@@ -51,7 +51,7 @@ class Slab(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("block", C.c_int32), ("tally_mode", C.c_int32), ("item_histories", C.c_int64),
                 ("sample_ms", C.c_float), ("candidates", C.c_int32), ("algorithm", C.c_int32),
-                ("steps_per_pass", C.c_int32)]
+                ("steps_per_pass", C.c_int32), ("defer", C.c_int32)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -96,6 +96,7 @@ def load_library(path=None):
         "mcg_simulate_source": (C.c_int, [vp, C.POINTER(Source), i64, i64]),
         "mcg_create_particles": (C.c_int, [vp, C.POINTER(Source), i64, i64, vp]),
         "mcg_worker_run": (C.c_int, [vp, C.POINTER(Source), i64, i32, i64, vp, vp]),
+        "mcg_worker_run_async": (C.c_int, [vp, C.POINTER(Source), i64, i64, vp]),
         "mcg_counters_read": (C.c_int, [vp, C.POINTER(Counters)]),
         "mcg_last_kernel_ms": (C.c_int, [vp, C.POINTER(C.c_float)]),
         "mcg_set_launch": (C.c_int, [vp, i32, i32, i32]),
@@ -112,6 +113,7 @@ def load_library(path=None):
         "mcg_fit_run": (C.c_int, [vp, i32, f32, f32, f32, f32, f32]),
         "mcg_fit_read": (C.c_int, [vp, vp, vp, vp]),
         "mcg_fit_release": (C.c_int, [vp]),
+        "mcg_fit_gradient": (C.c_int, [vp, vp, vp, vp]),
         "mcg_batch_set": (C.c_int, [vp, i32, vp, vp, vp, f32]),
         "mcg_batch_run": (C.c_int, [vp]),
         "mcg_batch_run_per_slab": (C.c_int, [vp]),
@@ -120,7 +122,10 @@ def load_library(path=None):
         "mcg_batch_set_launch": (C.c_int, [vp, i32, i64, i32]),
         "mcg_batch_autotune": (C.c_int, [vp, C.c_double, C.POINTER(Tuning)]),
         "mcg_batch_set_algorithm": (C.c_int, [vp, i32, i32]),
+        "mcg_batch_set_deferral": (C.c_int, [vp, i32]),
         "mcg_libm_eval_device": (C.c_int, [vp, C.c_int, vp, vp, i64]),
+        "mcg_testing_fail_allocation": (C.c_int, [i32]),
+        "mcg_measure_conversion_rates": (C.c_int, [vp, vp]),
         "mcg_verify_division": (C.c_int, [vp, C.c_int, C.c_uint64] + [C.POINTER(C.c_uint64)] * 3),
     }
     for name, (res, args) in sig.items():
@@ -340,6 +345,15 @@ class Context:
         _check(self.lib.mcg_fit_read(self.h, _ptr(sig), _ptr(loss), C.byref(st)))
         return sig, loss[:st.value]
 
+    def fit_gradient(self, weights):
+        """(weight absorbed per history, dF/dsig_a per history) of one
+        forward+adjoint launch of the fit's kernel with loss weights w."""
+        w = np.ascontiguousarray(weights, np.float64)
+        t = np.zeros(len(w), np.float64)
+        g = np.zeros(len(w), np.float64)
+        _check(self.lib.mcg_fit_gradient(self.h, _ptr(w), _ptr(t), _ptr(g)))
+        return t, g
+
     # -- batched slabs --
     def batch_set(self, slabs, sigs, rates, min_w):
         """slabs: list of dicts(n_cells, n_histories, base_seed, seed_mode, isotropic, mu0, w0);
@@ -377,6 +391,9 @@ class Context:
     def batch_set_launch(self, block=0, item_histories=0, tally_mode=-1):
         _check(self.lib.mcg_batch_set_launch(self.h, block, item_histories, tally_mode))
 
+    def batch_set_deferral(self, defer):
+        _check(self.lib.mcg_batch_set_deferral(self.h, 1 if defer else 0))
+
     def batch_set_algorithm(self, algorithm="history", steps_per_pass=0):
         _check(self.lib.mcg_batch_set_algorithm(self.h, 0 if algorithm == "history" else 1,
                                                 int(steps_per_pass)))
@@ -396,6 +413,20 @@ class Context:
                                        int(queue_capacity), C.byref(cyc), C.byref(hand)))
         return cyc.value, hand.value
 
+    def worker_run_async(self, n, queue_capacity=None, seed_mode=0, base_seed=5127801, x0=0.0,
+                         mu0=1.0, w0=1.0, isotropic=0, cell0=0):
+        """The asynchronous workers (one persistent launch, bounded on-device
+        rings); returns the number of hand-overs.  The default capacity per
+        ring is twice the GPU's resident threads."""
+        if queue_capacity is None:
+            import torch
+            queue_capacity = 2048 * torch.cuda.get_device_properties(0).multi_processor_count
+        src = Source(seed_mode, isotropic, base_seed, x0, mu0, w0, cell0)
+        hand = C.c_int64()
+        _check(self.lib.mcg_worker_run_async(self.h, C.byref(src), int(n), int(queue_capacity),
+                                             C.byref(hand)))
+        return hand.value
+
     def rnd_real_device(self, d_seeds, d_reals, n):
         _device_inputs_ready()
         _check(self.lib.mcg_rnd_real_device(self.h, C.c_void_p(d_seeds), C.c_void_p(d_reals), n))
@@ -406,6 +437,12 @@ class Context:
         c, m, x = C.c_uint64(), C.c_uint64(), C.c_uint64()
         _check(self.lib.mcg_verify_division(self.h, mode, n, C.byref(c), C.byref(m), C.byref(x)))
         return c.value, m.value, x.value
+
+    def conversion_rates(self):
+        """Measured conversions/s: u64->f32, f32->s64, u32->f32, f32->u32."""
+        r = np.zeros(4, np.float64)
+        _check(self.lib.mcg_measure_conversion_rates(self.h, _ptr(r)))
+        return dict(zip(("u64_f32", "f32_s64", "u32_f32", "f32_u32"), r.tolist()))
 
     def libm_eval_device(self, fn, d_in, d_out, n):
         _device_inputs_ready()

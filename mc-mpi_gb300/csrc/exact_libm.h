@@ -253,6 +253,11 @@ MCG_HD float mcg_exp_ff(float t, float *delta, const mcg_libm_tab *T)
   return mcg_exp_ff_core(t, delta, T);
 }
 
+/* |t| below this bound gives k = rint(RN(t * MCG_EXP_INV)) = 0
+ * (0.0054 * 92.3325 = 0.4986 < 1/2), so mcg_exp_ff_small(t) returns the bits
+ * of mcg_exp_ff_core(t) there. */
+#define MCG_EXP_SMALL_T 0.0054f
+
 /* Below this argument 1 - expf(t) rounds to exactly 1.0f whatever expf
  * returns (its result is below 2^-25); the table generator re-verifies this
  * against the host library for every float below the bound. */

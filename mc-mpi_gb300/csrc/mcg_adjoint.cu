@@ -12,6 +12,10 @@
  *  - sig_a enters only the weight attenuation exp(-sig_a l), never the flight
  *    sampling, so its derivative is pathwise:
  *        dG/dsig_a[c] = sum_{k: c_k = c} l_k (w_c W_k - (G - P_k));
+ *    this is a deliberate deviation from a score-function (likelihood-ratio)
+ *    estimator for sig_a: with implicit capture no sampled event depends on
+ *    sig_a, so its score is zero and the pathwise derivative is the whole
+ *    gradient (same expectation, far lower variance);
  *  - sig_s sets the flight distribution (exponential with rate sig_s): the
  *    log-density score of step k is 1/sig_s - l_k for a collision and -l_k
  *    for a crossing (no collision before the face), and it weights the loss

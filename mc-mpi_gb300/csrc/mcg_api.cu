@@ -3,6 +3,9 @@
  * libm exception tables, kernel launches and the C ABI of include/mcgb300.h.
  */
 #include <cuda_runtime.h>
+
+#include <atomic>
+#include <new>
 #include <dlfcn.h>
 
 #include <algorithm>
@@ -219,6 +222,8 @@ extern "C" int mcg_create(int device, int mode, mcg_context **out)
   return MCG_OK;
 }
 
+/* Releases the chain's device buffers and leaves the context with no
+ * geometry: launches and tally reads then return MCG_ERR_STATE. */
 static void free_geometry(mcg_context *ctx)
 {
   for (void *p : {(void *)ctx->d_cells_strict, (void *)ctx->d_cells_fast, (void *)ctx->d_tally})
@@ -226,6 +231,39 @@ static void free_geometry(mcg_context *ctx)
       cudaFree(p);
   ctx->d_cells_strict = ctx->d_cells_fast = nullptr;
   ctx->d_tally = nullptr;
+  ctx->n_layers = ctx->n_cells = ctx->cell_lo = 0;
+  ctx->layer_start.clear();
+  ctx->layer_m.clear();
+  ctx->layer_dx.clear();
+  ctx->sigs.clear();
+  ctx->rates.clear();
+  ctx->cells_strict.clear();
+  ctx->cells_fast.clear();
+  ctx->thin = false;
+}
+
+/* Allocations still to succeed before one is made to fail (-1: none). */
+static std::atomic<int> g_fail_alloc_in{-1};
+
+cudaError_t mcg_dev_malloc(void **p, size_t bytes)
+{
+  int k = g_fail_alloc_in.load();
+  while (k >= 0) {
+    if (g_fail_alloc_in.compare_exchange_weak(k, k - 1)) {
+      if (k == 0) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+      }
+      break;
+    }
+  }
+  return cudaMalloc(p, bytes);
+}
+
+extern "C" int mcg_testing_fail_allocation(int32_t after)
+{
+  g_fail_alloc_in.store(after < 0 ? -1 : after);
+  return MCG_OK;
 }
 
 static void free_scratch(mcg_context *ctx)
@@ -289,38 +327,66 @@ void mcg_cell_params(float sig, float rate, int gi, float dx, float4 &strict, fl
                      elo, ehi);
 }
 
+/* A chain is optically thin when every cell's absorption optical width
+ * sig_a (edge_hi - edge_lo) is at most 5e-4: a crossing then has
+ * |sig_a d_edge| >= MCG_EXP_SMALL_T (0.0054) only for |mu| < 0.093, which
+ * takes under 1 % of the crossings (their share of directions is about
+ * mu^2), so the strict tracker's certain-crossing path may evaluate the
+ * small-argument exp form alone and send the others to the full step. */
+static void update_thin(mcg_context *ctx)
+{
+  float widest = 0.0f;
+  for (const float4 &c : ctx->cells_strict)
+    widest = std::max(widest, std::fabs(c.x) * (c.w - c.z));
+  ctx->thin = !ctx->cells_strict.empty() && widest <= 5e-4f;
+}
+
 extern "C" int mcg_set_layers(mcg_context *ctx, int n_layers, const int32_t *h_index_start,
                               const int32_t *h_m, const float *h_dx, const float *h_sigs,
                               const float *h_rates, float particle_min_weight)
 {
   if (!ctx || n_layers <= 0 || !h_index_start || !h_m || !h_dx || !h_sigs || !h_rates)
     return mcg_fail(MCG_ERR_ARG, "mcg_set_layers: bad arguments");
-  int total = 0;
+  int64_t total64 = 0;
   for (int l = 0; l < n_layers; ++l) {
     if (h_m[l] <= 0)
       return mcg_fail(MCG_ERR_ARG, "mcg_set_layers: layer %d has %d cells", l, h_m[l]);
-    if (l > 0 && h_index_start[l] != h_index_start[l - 1] + h_m[l - 1])
+    if (l > 0 && (int64_t)h_index_start[l] != (int64_t)h_index_start[l - 1] + h_m[l - 1])
       return mcg_fail(MCG_ERR_ARG, "mcg_set_layers: layer %d is not contiguous", l);
-    total += h_m[l];
+    total64 += h_m[l];
+    if (total64 > INT32_MAX)
+      return mcg_fail(MCG_ERR_ARG, "mcg_set_layers: more than 2^31 - 1 cells");
   }
+  const int total = (int)total64;
   int rc = ensure_device(ctx);
   if (rc != MCG_OK)
     return rc;
-  std::vector<float4> cs(total), cf(total);
+  std::vector<float4> cs, cf;
+  try {
+    cs.resize(total);
+    cf.resize(total);
+  } catch (const std::bad_alloc &) {
+    return mcg_fail(MCG_ERR_ARG, "mcg_set_layers: no host memory for %d cells", total);
+  }
   int k = 0;
   for (int l = 0; l < n_layers; ++l)
     for (int j = 0; j < h_m[l]; ++j, ++k)
       mcg_cell_params(h_sigs[k], h_rates[k], h_index_start[l] + j, h_dx[l], cs[k], cf[k]);
   cudaStreamSynchronize(ctx->stream);
+  /* the old geometry goes first; any failure below leaves no geometry */
   free_geometry(ctx);
   cudaError_t e;
-  if ((e = cudaMalloc(&ctx->d_cells_strict, total * sizeof(float4))) != cudaSuccess ||
-      (e = cudaMalloc(&ctx->d_cells_fast, total * sizeof(float4))) != cudaSuccess ||
-      (e = cudaMalloc(&ctx->d_tally, total * sizeof(unsigned long long))) != cudaSuccess)
+  if ((e = mcg_dev_malloc((void **)&ctx->d_cells_strict, total * sizeof(float4))) != cudaSuccess ||
+      (e = mcg_dev_malloc((void **)&ctx->d_cells_fast, total * sizeof(float4))) != cudaSuccess ||
+      (e = mcg_dev_malloc((void **)&ctx->d_tally, total * sizeof(unsigned long long))) != cudaSuccess) {
+    free_geometry(ctx);
     return mcg_cuda_fail(e, "cudaMalloc(layers)");
+  }
   if ((e = cudaMemcpy(ctx->d_cells_strict, cs.data(), total * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess ||
-      (e = cudaMemcpy(ctx->d_cells_fast, cf.data(), total * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess)
+      (e = cudaMemcpy(ctx->d_cells_fast, cf.data(), total * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess) {
+    free_geometry(ctx);
     return mcg_cuda_fail(e, "cudaMemcpy(layers)");
+  }
   ctx->n_layers = n_layers;
   ctx->layer_start.assign(h_index_start, h_index_start + n_layers);
   ctx->layer_m.assign(h_m, h_m + n_layers);
@@ -329,6 +395,7 @@ extern "C" int mcg_set_layers(mcg_context *ctx, int n_layers, const int32_t *h_i
   ctx->rates.assign(h_rates, h_rates + total);
   ctx->cells_strict = cs;
   ctx->cells_fast = cf;
+  update_thin(ctx);
   ctx->n_cells = total;
   ctx->cell_lo = h_index_start[0];
   ctx->min_w = particle_min_weight;
@@ -343,12 +410,15 @@ extern "C" int mcg_set_layers_xs(mcg_context *ctx, int n_layers, const int32_t *
 {
   if (!ctx || n_layers <= 0 || !h_index_start || !h_m || !h_dx || !h_sig_a || !h_sig_s)
     return mcg_fail(MCG_ERR_ARG, "mcg_set_layers_xs: bad arguments");
-  int total = 0;
+  int64_t total64 = 0;
   for (int l = 0; l < n_layers; ++l) {
-    if (h_m[l] <= 0 || (l > 0 && h_index_start[l] != h_index_start[l - 1] + h_m[l - 1]))
+    if (h_m[l] <= 0 || (l > 0 && (int64_t)h_index_start[l] != (int64_t)h_index_start[l - 1] + h_m[l - 1]))
       return mcg_fail(MCG_ERR_ARG, "mcg_set_layers_xs: layer %d is empty or not contiguous", l);
-    total += h_m[l];
+    total64 += h_m[l];
+    if (total64 > INT32_MAX)
+      return mcg_fail(MCG_ERR_ARG, "mcg_set_layers_xs: more than 2^31 - 1 cells");
   }
+  const int total = (int)total64;
   std::vector<float> sigs(total), rates(total);
   for (int c = 0; c < total; ++c) {
     sigs[c] = h_sig_a[c] + h_sig_s[c];
@@ -367,12 +437,15 @@ extern "C" int mcg_set_layers_xs(mcg_context *ctx, int n_layers, const int32_t *
       cs.y = h_sig_s[k];
       cf.y = h_sig_s[k] > 1e-4f ? (float)(-0.69314718055994530942 / (double)h_sig_s[k]) : 0.0f;
     }
+  update_thin(ctx);
   cudaError_t e;
   if ((e = cudaMemcpy(ctx->d_cells_strict, ctx->cells_strict.data(), total * sizeof(float4),
                       cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(ctx->d_cells_fast, ctx->cells_fast.data(), total * sizeof(float4),
-                      cudaMemcpyHostToDevice)) != cudaSuccess)
+                      cudaMemcpyHostToDevice)) != cudaSuccess) {
+    free_geometry(ctx);
     return mcg_cuda_fail(e, "mcg_set_layers_xs: upload");
+  }
   return MCG_OK;
 }
 
@@ -566,15 +639,23 @@ int mcg_track_launch(mcg_context *ctx, mcg_particle *d_particles, int64_t n, int
   size_t smem = base + (tmode == MCG_TALLY_GLOBAL ? 0 : (size_t)ctx->n_cells * 8 * copies);
   P.tally_copies = copies;
   void (*kern)(mcg_track_params);
-  if (strict)
-    kern = tmode == MCG_TALLY_SMEM64 ? mcg_track_kernel<true, MCG_TALLY_SMEM64>
-         : tmode == MCG_TALLY_SMEM32 ? mcg_track_kernel<true, MCG_TALLY_SMEM32>
-                                     : mcg_track_kernel<true, MCG_TALLY_GLOBAL>;
+  if (strict && ctx->thin)
+    kern = tmode == MCG_TALLY_SMEM64 ? mcg_track_kernel<true, MCG_TALLY_SMEM64, true>
+         : tmode == MCG_TALLY_SMEM32 ? mcg_track_kernel<true, MCG_TALLY_SMEM32, true>
+                                     : mcg_track_kernel<true, MCG_TALLY_GLOBAL, true>;
+  else if (strict)
+    kern = tmode == MCG_TALLY_SMEM64 ? mcg_track_kernel<true, MCG_TALLY_SMEM64, false>
+         : tmode == MCG_TALLY_SMEM32 ? mcg_track_kernel<true, MCG_TALLY_SMEM32, false>
+                                     : mcg_track_kernel<true, MCG_TALLY_GLOBAL, false>;
   else
-    kern = tmode == MCG_TALLY_SMEM64 ? mcg_track_kernel<false, MCG_TALLY_SMEM64>
-         : tmode == MCG_TALLY_SMEM32 ? mcg_track_kernel<false, MCG_TALLY_SMEM32>
-                                     : mcg_track_kernel<false, MCG_TALLY_GLOBAL>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern = tmode == MCG_TALLY_SMEM64 ? mcg_track_kernel<false, MCG_TALLY_SMEM64, false>
+         : tmode == MCG_TALLY_SMEM32 ? mcg_track_kernel<false, MCG_TALLY_SMEM32, false>
+                                     : mcg_track_kernel<false, MCG_TALLY_GLOBAL, false>;
+  /* the limit is raised to the device's opt-in maximum, the same value on
+   * every call, so launches of the same kernel from other host threads (other
+   * contexts, the no-allocation entry point) cannot lower it under this one */
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       ctx->smem_optin);
   if (e != cudaSuccess)
     return mcg_cuda_fail(e, "cudaFuncSetAttribute");
   int bps = ctx->blocks_per_sm;

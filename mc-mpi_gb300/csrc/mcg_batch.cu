@@ -16,6 +16,7 @@
  * Layer::particle_step of src/layer.cpp:123-190.
  */
 #include <algorithm>
+#include <new>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -51,7 +52,7 @@ struct mcg_batch_params {
   uint32_t max_steps;
 };
 
-template <bool STRICT, int TALLY>
+template <bool STRICT, int TALLY, bool DEFER>
 __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -153,15 +154,32 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
          * unsigned compare is the slab's range test */
         const int kmax = (int)min((uint32_t)P.refill_steps, P.max_steps - nst);
         int k = 0;
-        bool going = true;
-        for (; k < kmax; ++k) {
-          if (!((wmc >= min_w) & ((unsigned)idx < (unsigned)m))) {
-            going = false;
-            break;
+        if (DEFER) {
+          /* certain crossings only; a lane whose step is anything else stops
+           * here, and the warp's stopped lanes complete their steps together
+           * below (mcg_step_cross + mcg_step_rest perform exactly mcg_step) */
+          bool rest = false;
+          while ((k < kmax) & (wmc >= min_w) & ((unsigned)idx < (unsigned)m)) {
+            if (!mcg_step_cross<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx,
+                                               __ldg(cells + idx), &tally[idx], qs, T, P.libm)) {
+              rest = true;
+              break;
+            }
+            ++k;
           }
-          mcg_step<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(cells + idx),
-                                  &tally[idx], qs, T, P.libm);
+          if (rest) {
+            mcg_step_rest<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(cells + idx),
+                                         &tally[idx], qs, T, P.libm);
+            ++k;
+          }
+        } else {
+          while ((k < kmax) & (wmc >= min_w) & ((unsigned)idx < (unsigned)m)) {
+            mcg_step<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(cells + idx),
+                                    &tally[idx], qs, T, P.libm);
+            ++k;
+          }
         }
+        const bool going = (wmc >= min_w) & ((unsigned)idx < (unsigned)m);
         nst += (uint32_t)k;
         if (!going || nst >= P.max_steps) {
           /* a history still alive in the slab here has reached the limit */
@@ -246,6 +264,8 @@ void mcg_ext_destroy(mcg_context *ctx)
     return;
   batch_free(&ctx->ext->batch);
   mcg_adjoint_release(&ctx->ext->adj);
+  if (ctx->ext->worker.dev)
+    cudaFree(ctx->ext->worker.dev);
   delete ctx->ext;
   ctx->ext = nullptr;
 }
@@ -270,14 +290,25 @@ extern "C" int mcg_batch_set(mcg_context *ctx, int32_t n_slabs, const mcg_slab *
   if (total > INT32_MAX || smem_need > (size_t)ctx->smem_optin)
     return mcg_fail(MCG_ERR_ARG, "mcg_batch_set: %lld cells / largest slab %d cells too large",
                     (long long)total, maxc);
+  std::vector<float4> cs, cf;
+  std::vector<mcg_batch_slab_dev> sd;
+  try {
+    cs.resize(total);
+    cf.resize(total);
+    sd.resize(n_slabs);
+  } catch (const std::bad_alloc &) {
+    return mcg_fail(MCG_ERR_ARG, "mcg_batch_set: no host memory for %lld cells", (long long)total);
+  }
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   mcg_batch_state *B = batch_of(ctx);
   const int keep_block = B->block, keep_tm = B->tally_mode;
+  const bool keep_defer = B->defer;
   const int64_t keep_item = B->item_histories;
   batch_free(B);
   B->block = keep_block;
   B->tally_mode = keep_tm;
+  B->defer = keep_defer;
   B->item_histories = keep_item;
   B->n_slabs = n_slabs;
   B->total_cells = (int)total;
@@ -286,8 +317,6 @@ extern "C" int mcg_batch_set(mcg_context *ctx, int32_t n_slabs, const mcg_slab *
   B->min_w = particle_min_weight;
   B->slabs.assign(h_slabs, h_slabs + n_slabs);
   B->cell_off.resize(n_slabs);
-  std::vector<float4> cs(total), cf(total);
-  std::vector<mcg_batch_slab_dev> sd(n_slabs);
   int64_t off = 0;
   for (int s = 0; s < n_slabs; ++s) {
     const mcg_slab &sl = h_slabs[s];
@@ -306,18 +335,28 @@ extern "C" int mcg_batch_set(mcg_context *ctx, int32_t n_slabs, const mcg_slab *
     sd[s].src.cell0 = 0;
     off += sl.n_cells;
   }
+  /* any failure from here on leaves no slabs set (launches return
+   * MCG_ERR_STATE), with the launch shape kept */
+  auto fail = [&](cudaError_t err, const char *what) {
+    batch_free(B);
+    B->block = keep_block;
+    B->tally_mode = keep_tm;
+    B->defer = keep_defer;
+    B->item_histories = keep_item;
+    return mcg_cuda_fail(err, what);
+  };
   cudaError_t e;
-  if ((e = cudaMalloc(&B->d_cells_strict, total * sizeof(float4))) != cudaSuccess ||
-      (e = cudaMalloc(&B->d_cells_fast, total * sizeof(float4))) != cudaSuccess ||
-      (e = cudaMalloc(&B->d_tally, total * sizeof(unsigned long long))) != cudaSuccess ||
-      (e = cudaMalloc(&B->d_slabs, n_slabs * sizeof(mcg_batch_slab_dev))) != cudaSuccess ||
-      (e = cudaMalloc(&B->d_item_next, 64)) != cudaSuccess)
-    return mcg_cuda_fail(e, "mcg_batch_set: cudaMalloc");
+  if ((e = mcg_dev_malloc((void **)&B->d_cells_strict, total * sizeof(float4))) != cudaSuccess ||
+      (e = mcg_dev_malloc((void **)&B->d_cells_fast, total * sizeof(float4))) != cudaSuccess ||
+      (e = mcg_dev_malloc((void **)&B->d_tally, total * sizeof(unsigned long long))) != cudaSuccess ||
+      (e = mcg_dev_malloc(&B->d_slabs, n_slabs * sizeof(mcg_batch_slab_dev))) != cudaSuccess ||
+      (e = mcg_dev_malloc((void **)&B->d_item_next, 64)) != cudaSuccess)
+    return fail(e, "mcg_batch_set: cudaMalloc");
   if ((e = cudaMemcpy(B->d_cells_strict, cs.data(), total * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(B->d_cells_fast, cf.data(), total * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(B->d_slabs, sd.data(), n_slabs * sizeof(mcg_batch_slab_dev), cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemset(B->d_tally, 0, total * sizeof(unsigned long long))) != cudaSuccess)
-    return mcg_cuda_fail(e, "mcg_batch_set: upload");
+    return fail(e, "mcg_batch_set: upload");
   return mcg_tally_reset(ctx) == MCG_OK ? MCG_OK : MCG_ERR_CUDA;
 }
 
@@ -396,14 +435,20 @@ static int batch_configure(mcg_context *ctx, mcg_batch_state *B, mcg_batch_launc
   const int tm = B->tally_mode;
   L.smem = sizeof(mcg_libm_tab) + 16 * 8 + 4 * 8 +
            (tm == MCG_TALLY_GLOBAL ? 0 : (size_t)B->max_cells * 8);
-  if (strict)
-    L.kern = tm == MCG_TALLY_SMEM64 ? mcg_batch_kernel<true, MCG_TALLY_SMEM64>
-           : tm == MCG_TALLY_SMEM32 ? mcg_batch_kernel<true, MCG_TALLY_SMEM32>
-                                    : mcg_batch_kernel<true, MCG_TALLY_GLOBAL>;
+  /* deferral is built for the shared-memory 32-bit tally (the autotuner's
+   * candidates); other tally modes run without it */
+  if (strict && B->defer && tm == MCG_TALLY_SMEM32)
+    L.kern = mcg_batch_kernel<true, MCG_TALLY_SMEM32, true>;
+  else if (!strict && B->defer && tm == MCG_TALLY_SMEM32)
+    L.kern = mcg_batch_kernel<false, MCG_TALLY_SMEM32, true>;
+  else if (strict)
+    L.kern = tm == MCG_TALLY_SMEM64 ? mcg_batch_kernel<true, MCG_TALLY_SMEM64, false>
+           : tm == MCG_TALLY_SMEM32 ? mcg_batch_kernel<true, MCG_TALLY_SMEM32, false>
+                                    : mcg_batch_kernel<true, MCG_TALLY_GLOBAL, false>;
   else
-    L.kern = tm == MCG_TALLY_SMEM64 ? mcg_batch_kernel<false, MCG_TALLY_SMEM64>
-           : tm == MCG_TALLY_SMEM32 ? mcg_batch_kernel<false, MCG_TALLY_SMEM32>
-                                    : mcg_batch_kernel<false, MCG_TALLY_GLOBAL>;
+    L.kern = tm == MCG_TALLY_SMEM64 ? mcg_batch_kernel<false, MCG_TALLY_SMEM64, false>
+           : tm == MCG_TALLY_SMEM32 ? mcg_batch_kernel<false, MCG_TALLY_SMEM32, false>
+                                    : mcg_batch_kernel<false, MCG_TALLY_GLOBAL, false>;
   cudaError_t e = cudaFuncSetAttribute(L.kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)L.smem);
   int bps = 0;
@@ -570,8 +615,8 @@ extern "C" int mcg_batch_run_per_slab(mcg_context *ctx)
     const int copies = ((size_t)sl.n_cells * 8 * warps <= 24 * 1024) ? warps : 1;
     P.tally_copies = copies;
     const size_t smem = sizeof(mcg_libm_tab) + 16 * 8 + (size_t)sl.n_cells * 8 * copies;
-    auto kern = strict ? mcg_track_kernel<true, MCG_TALLY_SMEM32>
-                       : mcg_track_kernel<false, MCG_TALLY_SMEM32>;
+    auto kern = strict ? mcg_track_kernel<true, MCG_TALLY_SMEM32, false>
+                       : mcg_track_kernel<false, MCG_TALLY_SMEM32, false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     int bps = 1;
@@ -657,6 +702,16 @@ extern "C" int mcg_batch_set_launch(mcg_context *ctx, int32_t block, int64_t ite
   return MCG_OK;
 }
 
+extern "C" int mcg_batch_set_deferral(mcg_context *ctx, int32_t defer)
+{
+  if (!ctx || (defer != 0 && defer != 1))
+    return mcg_fail(MCG_ERR_ARG, "mcg_batch_set_deferral: bad arguments");
+  mcg_batch_state *B = batch_of(ctx);
+  B->defer = defer != 0;
+  B->graph_valid = false;
+  return MCG_OK;
+}
+
 extern "C" int mcg_batch_set_algorithm(mcg_context *ctx, int32_t algorithm, int32_t steps_per_pass)
 {
   if (!ctx || (algorithm != MCG_ALGO_HISTORY && algorithm != MCG_ALGO_EVENT) || steps_per_pass < 0)
@@ -677,7 +732,8 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
     return mcg_fail(MCG_ERR_ARG, "mcg_batch_autotune: sample fraction must be in (0, 1]");
   const int blocks[] = {256, 512, 1024};
   const int64_t items[] = {4096, 16384, 65536};
-  const int tmodes[] = {MCG_TALLY_SMEM32, MCG_TALLY_SMEM64};
+  /* tally mode and deferral of the full step */
+  const int shapes[][2] = {{MCG_TALLY_SMEM32, 0}, {MCG_TALLY_SMEM32, 1}, {MCG_TALLY_SMEM64, 0}};
   /* every candidate runs the same sample, of at least four times the event
    * engine's drain size (below it the event-based form is a single drain
    * launch, and a persistent launch is dominated by its tail), or the whole
@@ -694,7 +750,7 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
   double best = 1e30; /* ms per history */
   int nc = 0;
   mcg_batch_tuning pick = {B->block, B->tally_mode, B->item_histories, 0.f, 0, MCG_ALGO_HISTORY,
-                           0};
+                           0, B->defer ? 1 : 0};
   bool warmed = false;
   for (int64_t it : items) {
     /* the sample keeps the full run's number of items per slab, so the
@@ -703,9 +759,11 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
     if ((rc = build_items(ctx, B, sample_item, sample_fraction)) != MCG_OK)
       return rc;
     for (int bl : blocks)
-      for (int tm : tmodes) {
+      for (const auto &sh : shapes) {
+        const int tm = sh[0];
         B->block = bl;
         B->tally_mode = tm;
+        B->defer = sh[1] != 0;
         mcg_batch_launch L;
         if ((rc = batch_configure(ctx, B, L)) != MCG_OK)
           return rc;
@@ -721,7 +779,7 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
         ++nc;
         if (ctx->last_ms / (double)n_hist < best) {
           best = ctx->last_ms / (double)n_hist;
-          pick = {bl, tm, it, ctx->last_ms, 0, MCG_ALGO_HISTORY, 0};
+          pick = {bl, tm, it, ctx->last_ms, 0, MCG_ALGO_HISTORY, 0, sh[1]};
         }
       }
   }
@@ -733,7 +791,7 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
     ++nc;
     if (ctx->last_ms / (double)n_event < best) {
       best = ctx->last_ms / (double)n_event;
-      pick = {B->block, B->tally_mode, B->item_histories, ctx->last_ms, 0, MCG_ALGO_EVENT, k};
+      pick = {B->block, B->tally_mode, B->item_histories, ctx->last_ms, 0, MCG_ALGO_EVENT, k, 0};
     }
   }
   B->algorithm = pick.algorithm;
@@ -742,6 +800,7 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
   B->block = pick.block;
   B->tally_mode = pick.tally_mode;
   B->item_histories = pick.item_histories;
+  B->defer = pick.defer != 0;
   B->items_built_for = -1;
   B->graph_valid = false;
   pick.candidates = nc;

@@ -48,15 +48,21 @@ __device__ __forceinline__ float mcg_u63_unit(uint64_t s)
   return __uint_as_float(((uint32_t)(126 - lz) << 23) + mant + up);
 }
 
-/* rnd_real: s <- (G s + C) mod 2^63; h = RN((float)s) * 2^-63.
- * The hardware conversion issues on the FP64 pipe (about 6e11 64-bit
- * conversions/s per GB300); with this one and the deposit's per step it is
- * the strict tracker's tightest resource, yet the integer version
- * (MCG_INT_CONVERSIONS, same bits) costs more issue slots than it frees
- * (measured +31 % steps/s for the hardware form when it was introduced). */
-__device__ __forceinline__ float mcg_rnd_real(uint64_t &s)
+/* The reference's LCG step s <- (G s + C) mod 2^63 (src/random.cpp:14). */
+__device__ __forceinline__ void mcg_lcg_next(uint64_t &s)
 {
   s = (MCG_RNG_G * s + MCG_RNG_C) & MCG_MASK63;
+}
+
+/* rnd_real's value of a state s < 2^63: RN((float)s) * 2^-63
+ * (src/random.cpp:15).  The hardware u64 -> f32 conversion issues on the
+ * FP64 pipe (about 6e11 conversions/s per GB300), so the trackers call this
+ * only where the float value itself is needed (scatters, near-ties, the
+ * source's directions); the certain-crossing test compares the state's top
+ * bits as an integer instead (mcg_cross_threshold).  MCG_INT_CONVERSIONS
+ * selects the integer version (same bits). */
+__device__ __forceinline__ float mcg_unit_of(uint64_t s)
+{
 #ifdef MCG_INT_CONVERSIONS
   return mcg_u63_unit(s);
 #else
@@ -64,18 +70,22 @@ __device__ __forceinline__ float mcg_rnd_real(uint64_t &s)
 #endif
 }
 
-/* Fast arithmetic's uniform: the same LCG step, then the state's top 23
- * bits k as the midpoint (k + 1/2) 2^-23 of their interval (two
- * integer/float operations instead of an exact 64-bit rounding).  The
+/* rnd_real: s <- (G s + C) mod 2^63; h = RN((float)s) * 2^-63. */
+__device__ __forceinline__ float mcg_rnd_real(uint64_t &s)
+{
+  mcg_lcg_next(s);
+  return mcg_unit_of(s);
+}
+
+/* Fast arithmetic's uniform for directions: the same LCG step, then the
+ * state's top 23 bits k as the midpoint (k + 1/2) 2^-23 of their interval
+ * (two integer/float operations instead of an exact 64-bit rounding).  The
  * subtraction from [1, 2) of 1 - 2^-24 is exact (Sterbenz).  The midpoint
- * keeps the flight test unbiased: truncating to k 2^-23 put h half a step
- * low, which on fine meshes (collision probability per crossing ~1e-4)
- * lowered every cell's collision rate by ~2e-4 relative, a shift of
- * several standard errors at 1e8 histories; it also makes mu = 2h - 1
- * symmetric about 0 and h never 0. */
+ * makes mu = 2h - 1 symmetric about 0 and h never 0.  (Flight samples use
+ * mcg_flight_log2, at 2^-32 resolution.) */
 __device__ __forceinline__ float mcg_rnd_real_fast(uint64_t &s)
 {
-  s = (MCG_RNG_G * s + MCG_RNG_C) & MCG_MASK63;
+  mcg_lcg_next(s);
   return __fsub_rn(__uint_as_float(0x3f800000u | (uint32_t)(s >> 40)), 0x1.fffffep-1f);
 }
 
@@ -107,29 +117,54 @@ __device__ __forceinline__ float mcg_ex2_approx(float x)
 }
 
 /* Certain-crossing test of the strict tracker.  The reference samples
- * di = RN(-logf(h) / sig_i) and crosses when !(di < de).  The tracker first
- * tests  h < E,  E = RN(ex2(RN(RN(sig_i de) * -log2(e))) * MCG_CROSS_FACTOR),
- * and only evaluates the exact logarithm when the test fails.
+ * h = RN((float)s) 2^-63, di = RN(-logf(h) / sig_i) and crosses when
+ * !(di < de).  The tracker first tests, on the state s itself,
+ *     floor(s / 2^32) < B,   B = trunc(RN(E * K)),
+ *     E = ex2(RN(RN(sig_i de) * -log2(e))),  K = 2^31 (1 - m), m = 2^-14,
+ * with one MUFU operation and one 32-bit conversion (no 64-bit one), and
+ * only evaluates h and the exact logarithm when the test fails.
  *
- * Why h < E implies the crossing (T = sig_i de exactly, u = 2^-24):
+ * Why the test implies the crossing (T = sig_i de exactly, u = 2^-24):
+ *  - s < (floor(s / 2^32) + 1) 2^32 <= B 2^32 <= E (1 - m)(1 + u) 2^63, and
+ *    RN is monotonic, so h <= E (1 - m)(1 + u)^2;
  *  - the two roundings and RN(log2 e) give an exponent T log2(e) (1 + eps)
  *    with |eps| <= 3.01 u, so 2^exponent lies within a factor
  *    exp(+-T |eps|) of e^-T;
  *  - ex2.approx is at most 2^-20 above 2^x (exhaustively checked over every
- *    argument the test can see by the GPU tests); the last product adds u;
- *  - h >= 2^-63 when nonzero, so h < E forces T < 44;
- *  - hence -ln h > T + m - 2^-20 - u - m^2 - 44 |eps|, m = 1 - FACTOR = 2^-14,
- *    and with the host logf within rho = 2^-22 relative of ln (verified
- *    exhaustively when the exception table is built):
- *    -logf(h) >= -ln(h) (1 - rho) > T + m - 2^-20 - u - m^2 - 44 (|eps| + rho) > T,
- *    so the exact quotient -logf(h) / sig_i is at least de and its rounding,
- *    RN being monotonic and de a float, is too;
- *  - h == 0 gives -logf(0) = inf, a crossing for the reference as well.
+ *    argument the test can see by the GPU tests);
+ *  - h >= 2^-63 when nonzero, so the test passing forces T < 44;
+ *  - hence -ln h > T + m - 2^-20 - 2u - m^2 - 44 |eps|, and with the host
+ *    logf within rho = 2^-22 relative of ln (verified exhaustively when the
+ *    exception table is built):
+ *    -logf(h) >= -ln(h) (1 - rho) > T + m - 2^-20 - 2u - m^2 - 44 (|eps| + rho) > T
+ *    (m = 6.1e-5 against 2.0e-5 for the rest), so the exact quotient
+ *    -logf(h) / sig_i is at least de and its rounding, RN being monotonic
+ *    and de a float, is too;
+ *  - h == 0 gives -logf(0) = inf, a crossing for the reference as well;
+ *  - sig_i <= EPS: the reference crosses whatever h is (di = MAXREAL), so
+ *    the test may pass there too; sig_i or de NaN or infinite gives E NaN or
+ *    0 and B = 0 (the conversion takes NaN to 0), which fails.
  * A false result only costs the exact evaluation: the exact path decides
  * every case the test does not settle (about 2e-5 of crossings). */
 #define MCG_LOG2E_F 1.44269502f
 #define MCG_CROSS_FACTOR 0.99993896484375f /* 1 - 2^-14 */
+#define MCG_CROSS_SCALE 2147352576.0f      /* 2^31 (1 - 2^-14) = 2^31 - 2^17, exact */
 #define MCG_LOGF_RELERR_MAX 0x1p-22f       /* rho above, checked at table load */
+
+/* B of the certain-crossing test for a flight of length de in a cell of
+ * interaction cross section sig_i (the truncating conversion saturates: B is
+ * 0 for NaN and 2^32 - 1 above the range, where s < 2^63 always passes). */
+__device__ __forceinline__ uint32_t mcg_cross_threshold(float sig_i, float de)
+{
+  const float e = mcg_ex2_approx(__fmul_rn(__fmul_rn(sig_i, de), -MCG_LOG2E_F));
+  return __float2uint_rz(__fmul_rn(e, MCG_CROSS_SCALE));
+}
+
+/* The state's top 31 bits, floor(s / 2^32), compared against B. */
+__device__ __forceinline__ uint32_t mcg_state_hi(uint64_t s)
+{
+  return (uint32_t)(s >> 32);
+}
 
 __device__ __forceinline__ uint64_t mcg_rnd_seed(uint64_t &s)
 {
@@ -246,12 +281,31 @@ __device__ __forceinline__ float mcg_expf_strict(float t, const mcg_libm_tab *T,
   return y;
 }
 
-/* log2(h) of the fast arithmetic's flight sample h in (0, 1).  The hardware
- * log2 is documented to an absolute error of 2^-22 on [0.5, 2]; near 1,
- * where -log h is as small as a thin cell's collision probability (~1e-4 on
- * a 10,000-cell slab), that is a relative error of a few 1e-4 in the flight
- * test.  For u = 1 - h < 2^-8 (u exact) the series -ln(1 - u) = u (1 + u/2 +
- * u^2/3) (truncation below 2^-26 relative) is used instead. */
+/* log2(h) of the fast arithmetic's flight sample, drawn from the state s
+ * (already advanced) at 2^-32 resolution: t = the state's top 32 bits,
+ * h = (t + 1/2) 2^-32, u = 1 - h = (~t + 1/2) 2^-32.  A thin cell's collision
+ * probability per crossing is ~1e-4 (10,000-cell slab), decided by u within
+ * ~1e-4 of 0, so u must be fine-grained there: on a 2^-23 grid it shifts each
+ * cell's collision probability by up to half a grid step (3e-4 relative rms
+ * per cell against the reference's 2^-24 grid), a 2^-32 grid by ~1e-6.
+ * Near 1 (u < 2^-8, u exact below 2^-9 and within 2^-24 relative above) the
+ * series -ln(1 - u) = u (1 + u/2 + u^2/3) (truncation below 2^-26
+ * relative); elsewhere the hardware log2 of h = RN(1 - u), documented to an
+ * absolute error of 2^-22 on [0.5, 2], which near 1 would be a relative error
+ * of a few 1e-4 in the flight test. */
+__device__ __forceinline__ float mcg_flight_log2(uint64_t s)
+{
+  const uint32_t t = (uint32_t)(s >> 31);
+  const float u = __fmaf_rn(__uint2float_rn(~t), 0x1p-32f, 0x1p-33f);
+  float p = fmaf(u, MCG_LOG2E_F * (1.0f / 3.0f), MCG_LOG2E_F * 0.5f);
+  p = fmaf(u, p, MCG_LOG2E_F);
+  const float near1 = -u * p;
+  return u < 0x1p-8f ? near1 : __log2f(__fsub_rn(1.0f, u));
+}
+
+/* The former flight log2 on a float sample h in (0, 1) (the midpoint grid
+ * of mcg_rnd_real_fast): the series for u = 1 - h < 2^-8, else the hardware
+ * log2.  Kept as a testing aid (mcg_libm_eval_device fn 5). */
 __device__ __forceinline__ float mcg_log2_flight(float h)
 {
   const float u = __fsub_rn(1.0f, h);
@@ -306,6 +360,12 @@ __device__ __forceinline__ long long mcg_to_fixed(float dw, int S)
     q = 0; /* below one half unit */
   }
   return (u >> 31) ? -(long long)q : (long long)q;
+}
+
+/* The scale 2^S as a float (0 <= S <= 62). */
+__device__ __forceinline__ float mcg_fixed_scale(int S)
+{
+  return __int_as_float((127 + S) << 23);
 }
 
 __device__ __forceinline__ unsigned lanemask_lt()

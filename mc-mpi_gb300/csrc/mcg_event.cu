@@ -7,13 +7,14 @@
  *   1. flight kernel: every live particle draws its flight sample; a certain
  *      crossing (the common event of a fine mesh) is completed at once, up to
  *      K of them per pass; a particle whose event is not a certain crossing
- *      is moved, with its sample, into the collision queue; survivors are
+ *      is moved into the collision queue, its state advanced to the
+ *      flight sample's (which determines the sample); survivors are
  *      compacted into the other bank.  Threads take four consecutive
  *      particles and read each field with one 128-bit load; warp ballots and
  *      popc give every survivor and every queued particle its slot, one
  *      atomic per warp and destination reserves the warp's range;
  *   2. collision kernel: the queued events (scatters, near-ties, the
- *      reference's EPS cases) complete their step from the stored sample in
+ *      reference's EPS cases) complete their step from that state in
  *      converged warps and join the bank;
  *   3. newborns from the source top the bank up to its capacity.
  * When the source is exhausted and fewer particles than a full grid remain,
@@ -26,7 +27,7 @@
  *
  * The engine serves one chain (mcg_set_algorithm) and the batched slabs
  * (mcg_batch_set_algorithm; the bank then carries the slab index).
- * Memory per particle and pass: 36 B read + 36 B written (+ 40 B each way
+ * Memory per particle and pass: 36 B read + 36 B written (+ 36 B each way
  * through the queue for a collision).
  */
 #include <algorithm>
@@ -65,12 +66,12 @@ struct mcg_ev_params {
 /* A lane's particle. */
 struct mcg_ev_particle {
   uint64_t seed;
-  float x, mu, wmc, h;
+  float x, mu, wmc;
   int32_t idx, hid, nst, nsc;
 };
 
 __device__ __forceinline__ void mcg_ev_store(const mcg_soa &b, unsigned long long i,
-                                             const mcg_ev_particle &p, bool with_h)
+                                             const mcg_ev_particle &p)
 {
   b.seed[i] = p.seed;
   b.x[i] = p.x;
@@ -80,14 +81,12 @@ __device__ __forceinline__ void mcg_ev_store(const mcg_soa &b, unsigned long lon
   b.hid[i] = p.hid;
   b.nst[i] = p.nst;
   b.nsc[i] = p.nsc;
-  if (with_h)
-    b.h[i] = p.h;
 }
 
 /* Particles 4q..4q+3 of a bank (those below n), 128-bit loads for full quads. */
 __device__ __forceinline__ void mcg_ev_load4(const mcg_soa &b, unsigned long long q,
                                              unsigned long long n, mcg_ev_particle p[4],
-                                             bool live[4], bool with_h)
+                                             bool live[4])
 {
   const unsigned long long i0 = 4 * q;
   if (i0 + 3 < n) {
@@ -108,10 +107,6 @@ __device__ __forceinline__ void mcg_ev_load4(const mcg_soa &b, unsigned long lon
     p[0].hid = vh.x, p[1].hid = vh.y, p[2].hid = vh.z, p[3].hid = vh.w;
     p[0].nst = vs.x, p[1].nst = vs.y, p[2].nst = vs.z, p[3].nst = vs.w;
     p[0].nsc = vc.x, p[1].nsc = vc.y, p[2].nsc = vc.z, p[3].nsc = vc.w;
-    if (with_h) {
-      const float4 vq = reinterpret_cast<const float4 *>(b.h)[q];
-      p[0].h = vq.x, p[1].h = vq.y, p[2].h = vq.z, p[3].h = vq.w;
-    }
 #pragma unroll
     for (int j = 0; j < 4; ++j)
       live[j] = true;
@@ -129,8 +124,6 @@ __device__ __forceinline__ void mcg_ev_load4(const mcg_soa &b, unsigned long lon
         p[j].hid = b.hid[i];
         p[j].nst = b.nst[i];
         p[j].nsc = b.nsc[i];
-        if (with_h)
-          p[j].h = b.h[i];
       }
     }
   }
@@ -231,7 +224,7 @@ __device__ __forceinline__ void mcg_ev_flush_tally(const mcg_ev_params &P,
 /* Warp-compacted append of the lanes with `want` to a bank; one atomic per
  * warp on *count reserves the warp's range. */
 __device__ __forceinline__ void mcg_ev_append(const mcg_soa &b, unsigned long long *count,
-                                              bool want, const mcg_ev_particle &p, bool with_h)
+                                              bool want, const mcg_ev_particle &p)
 {
   const unsigned ball = __ballot_sync(0xffffffffu, want);
   if (!ball)
@@ -242,11 +235,11 @@ __device__ __forceinline__ void mcg_ev_append(const mcg_soa &b, unsigned long lo
     base = atomicAdd(count, (unsigned long long)__popc(ball));
   base = __shfl_sync(0xffffffffu, base, __ffs(ball) - 1);
   if (want)
-    mcg_ev_store(b, base + __popc(ball & lanemask_lt()), p, with_h);
+    mcg_ev_store(b, base + __popc(ball & lanemask_lt()), p);
 }
 
 /* Pass part 1: certain crossings, up to K per particle; other events go to
- * the collision queue with their flight sample. */
+ * the collision queue with their state advanced to the flight sample's. */
 template <bool STRICT, bool SLABS, bool SMEM>
 __global__ void __launch_bounds__(MCG_EV_BLOCK, MCG_EV_MIN_BLOCKS) mcg_ev_flight_kernel(mcg_ev_params P)
 {
@@ -270,7 +263,7 @@ __global__ void __launch_bounds__(MCG_EV_BLOCK, MCG_EV_MIN_BLOCKS) mcg_ev_flight
        base += (unsigned long long)gridDim.x * blockDim.x) {
     mcg_ev_particle p[4];
     bool live[4], queued[4];
-    mcg_ev_load4(P.in, base + tid, n, p, live, false);
+    mcg_ev_load4(P.in, base + tid, n, p, live);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       queued[j] = false;
@@ -291,12 +284,9 @@ __global__ void __launch_bounds__(MCG_EV_BLOCK, MCG_EV_MIN_BLOCKS) mcg_ev_flight
           ended = true;
           break;
         }
-        float h;
         if (!mcg_step_cross<STRICT, SMEM ? MCG_TALLY_SMEM32 : MCG_TALLY_GLOBAL>(p[j].seed, p[j].x, p[j].mu, p[j].wmc,
                                                       inv_mu, p[j].idx, __ldg(cells + p[j].idx),
-                                                      &tally[p[j].idx], P.q_log2, &T, P.libm,
-                                                      h)) {
-          p[j].h = h;
+                                                      &tally[p[j].idx], P.q_log2, &T, P.libm)) {
           queued[j] = true;
           break;
         }
@@ -316,8 +306,8 @@ __global__ void __launch_bounds__(MCG_EV_BLOCK, MCG_EV_MIN_BLOCKS) mcg_ev_flight
     }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      mcg_ev_append(P.out, &P.ctl->n_out, live[j], p[j], false);
-      mcg_ev_append(P.q, &P.ctl->n_q, queued[j], p[j], true);
+      mcg_ev_append(P.out, &P.ctl->n_out, live[j], p[j]);
+      mcg_ev_append(P.q, &P.ctl->n_q, queued[j], p[j]);
     }
   }
   mcg_ev_flush_counters(P, s_cnt, steps, 0ull);
@@ -349,7 +339,7 @@ __global__ void __launch_bounds__(MCG_EV_BLOCK, MCG_EV_MIN_BLOCKS) mcg_ev_collid
        base += (unsigned long long)gridDim.x * blockDim.x) {
     mcg_ev_particle p[4];
     bool live[4];
-    mcg_ev_load4(P.q, base + tid, n, p, live, true);
+    mcg_ev_load4(P.q, base + tid, n, p, live);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       if (!live[j])
@@ -362,7 +352,7 @@ __global__ void __launch_bounds__(MCG_EV_BLOCK, MCG_EV_MIN_BLOCKS) mcg_ev_collid
         tally = s_tally;
       float inv_mu = mcg_flight_rcp(p[j].mu);
       uint32_t sc = (uint32_t)p[j].nsc;
-      mcg_step_rest<STRICT, SMEM ? MCG_TALLY_SMEM32 : MCG_TALLY_GLOBAL>(p[j].h, p[j].seed, p[j].x, p[j].mu, p[j].wmc, inv_mu,
+      mcg_step_rest<STRICT, SMEM ? MCG_TALLY_SMEM32 : MCG_TALLY_GLOBAL>(p[j].seed, p[j].x, p[j].mu, p[j].wmc, inv_mu,
                                               p[j].idx, sc, __ldg(cells + p[j].idx),
                                               &tally[p[j].idx], P.q_log2, &T, P.libm);
       scat += sc - (uint32_t)p[j].nsc;
@@ -377,7 +367,7 @@ __global__ void __launch_bounds__(MCG_EV_BLOCK, MCG_EV_MIN_BLOCKS) mcg_ev_collid
     }
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-      mcg_ev_append(P.out, &P.ctl->n_out, live[j], p[j], false);
+      mcg_ev_append(P.out, &P.ctl->n_out, live[j], p[j]);
   }
   mcg_ev_flush_counters(P, s_cnt, steps, scat);
   if (SMEM)
@@ -431,8 +421,7 @@ __global__ void mcg_ev_birth_kernel(mcg_ev_params P)
     }
     p.idx = idx;
     p.nst = p.nsc = 0;
-    p.h = 0.f;
-    mcg_ev_store(P.out, base + i, p, false);
+    mcg_ev_store(P.out, base + i, p);
   }
 }
 
@@ -500,14 +489,14 @@ static int soa_alloc(mcg_soa &s, size_t cap, std::vector<void *> &owned)
   void *base = nullptr;
   /* one allocation, each field 256-byte aligned (128-bit loads of quads) */
   const size_t pad = (cap + 63) & ~(size_t)63;
-  cudaError_t e = cudaMalloc(&base, pad * (8 + 8 * 4));
+  cudaError_t e = cudaMalloc(&base, pad * (8 + 7 * 4));
   if (e != cudaSuccess)
     return mcg_cuda_fail(e, "event buffers");
   owned.push_back(base);
   char *p = static_cast<char *>(base);
   s.seed = reinterpret_cast<unsigned long long *>(p);
   p += pad * 8;
-  float **f[4] = {&s.x, &s.mu, &s.wmc, &s.h};
+  float **f[3] = {&s.x, &s.mu, &s.wmc};
   for (float **q : f) {
     *q = reinterpret_cast<float *>(p);
     p += pad * 4;

@@ -489,3 +489,56 @@ extern "C" int mcg_fit_read(mcg_context *ctx, float *h_sig_a, double *h_loss_his
     *h_steps = (int32_t)st;
   return MCG_OK;
 }
+
+/* One batched forward + adjoint launch of the fit kernel at the current
+ * sig_a with the given loss weights (testing aid): histories step * n + i of
+ * every slab, as the next Adam step would run, with w_c = h_weights[c]
+ * instead of 2 (a_c - t_c).  Returns per cell the weight absorbed per history
+ * (h_tally) and dF/dsig_a per history (h_grad), F = sum_c w_c a_c, so the
+ * fit's gradient can be compared with mcg_adjoint's on the same histories.
+ * The fit's own loss weights and accumulators are left as they were. */
+extern "C" int mcg_fit_gradient(mcg_context *ctx, const double *h_weights, double *h_tally,
+                                double *h_grad)
+{
+  mcg_fit_state *F = ctx ? fit_of(ctx, false) : nullptr;
+  if (!F)
+    return mcg_fail(MCG_ERR_STATE, "mcg_fit_gradient: mcg_fit_set first");
+  if (!h_weights || !h_tally || !h_grad)
+    return mcg_fail(MCG_ERR_ARG, "mcg_fit_gradient: bad arguments");
+  cudaSetDevice(ctx->device);
+  const int n = F->n_cells;
+  std::vector<float2> saved(n), ax(n);
+  std::vector<double> keep_grad(n);
+  std::vector<unsigned long long> keep_tally(n), q(n);
+  std::vector<mcg_fit_slab_dev> sd(F->n_slabs);
+  std::vector<int32_t> cs(n);
+  for (int c = 0; c < n; ++c)
+    ax[c] = make_float2((float)h_weights[c], 0.0f);
+  cudaError_t e;
+  if ((e = cudaMemcpy(saved.data(), F->aux, n * sizeof(float2), cudaMemcpyDeviceToHost)) != cudaSuccess ||
+      (e = cudaMemcpy(keep_grad.data(), F->grad, n * 8, cudaMemcpyDeviceToHost)) != cudaSuccess ||
+      (e = cudaMemcpy(keep_tally.data(), F->tally, n * 8, cudaMemcpyDeviceToHost)) != cudaSuccess ||
+      (e = cudaMemcpy(sd.data(), F->slabs, F->n_slabs * sizeof(mcg_fit_slab_dev), cudaMemcpyDeviceToHost)) != cudaSuccess ||
+      (e = cudaMemcpy(cs.data(), F->cell_slab, n * 4, cudaMemcpyDeviceToHost)) != cudaSuccess ||
+      (e = cudaMemcpy(F->aux, ax.data(), n * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemset(F->grad, 0, n * 8)) != cudaSuccess ||
+      (e = cudaMemset(F->tally, 0, n * 8)) != cudaSuccess)
+    return mcg_cuda_fail(e, "mcg_fit_gradient: set-up");
+  int rc = fit_launch_track(ctx, F, 1);
+  if (rc != MCG_OK)
+    return rc;
+  if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess ||
+      (e = cudaMemcpy(q.data(), F->tally, n * 8, cudaMemcpyDeviceToHost)) != cudaSuccess ||
+      (e = cudaMemcpy(h_grad, F->grad, n * 8, cudaMemcpyDeviceToHost)) != cudaSuccess ||
+      (e = cudaMemcpy(F->aux, saved.data(), n * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(F->grad, keep_grad.data(), n * 8, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(F->tally, keep_tally.data(), n * 8, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return mcg_cuda_fail(e, "mcg_fit_gradient");
+  const double inv_scale = std::ldexp(1.0, -ctx->log2_scale);
+  for (int c = 0; c < n; ++c) {
+    const double nh = (double)sd[cs[c]].n_hist;
+    h_tally[c] = (double)(long long)q[c] * inv_scale / nh;
+    h_grad[c] /= nh;
+  }
+  return MCG_OK;
+}

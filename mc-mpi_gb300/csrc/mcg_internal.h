@@ -29,6 +29,7 @@ struct mcg_batch_state {
   float min_w = 0.f;
   /* launch shape, chosen by mcg_batch_set_launch or the autotuner */
   int block = 512, tally_mode = 1;
+  bool defer = false; /* deferral of the full step (mcg_batch_set_deferral) */
   int64_t item_histories = 16384;
   /* history- or event-based; events per pass of the event engine */
   int algorithm = MCG_ALGO_HISTORY, event_steps = 8;
@@ -51,21 +52,29 @@ struct mcg_adj_state {
 
 struct mcg_fit_state; /* mcg_fit.cu */
 
+/* Device buffers of the workers' forms (mcg_worker.cu), kept between calls
+ * and grown on demand, so a Worker called repeatedly allocates nothing. */
+struct mcg_worker_state {
+  void *dev = nullptr;
+  size_t bytes = 0;
+};
+
 struct mcg_ext {
   mcg_batch_state batch;
   mcg_adj_state adj;
   mcg_fit_state *fit = nullptr;
+  mcg_worker_state worker;
 };
 
 /* Structure-of-arrays particle buffer of the event-based tracker: per
  * particle the state, the cell index local to its chain or slab, the history
- * (chain) or slab (batched) it belongs to, its step and scatter counts, and
- * in the collision queue the flight sample already drawn. */
+ * (chain) or slab (batched) it belongs to, and its step and scatter counts.
+ * In the collision queue the seed is already advanced to the flight
+ * sample's state, which determines the sample. */
 struct mcg_soa {
   unsigned long long *seed;
   float *x, *mu, *wmc;
   int32_t *idx, *hid, *nst, *nsc;
-  float *h;
 };
 
 /* Counters of the event engine, on the device. */
@@ -97,6 +106,7 @@ struct mcg_context {
   std::vector<int32_t> layer_start, layer_m;
   std::vector<float> layer_dx, sigs, rates;
   std::vector<float4> cells_strict, cells_fast;
+  bool thin = false; /* every cell's sig_a width <= 5e-4 (mcg_step THIN) */
   float4 *d_cells_strict = nullptr, *d_cells_fast = nullptr;
   unsigned long long *d_tally = nullptr;
   int log2_scale = 40;
@@ -131,6 +141,10 @@ struct mcg_context {
 };
 
 int mcg_fail(int code, const char *fmt, ...);
+/* cudaMalloc of the geometry set-up (mcg_set_layers, mcg_batch_set); a test
+ * can make one of them report cudaErrorMemoryAllocation without attempting
+ * it (mcg_testing_fail_allocation). */
+cudaError_t mcg_dev_malloc(void **p, size_t bytes);
 int mcg_cuda_fail(cudaError_t e, const char *what);
 void mcg_cell_params(float sig, float rate, int gi, float dx, float4 &strict, float4 &fast);
 int mcg_track_launch(mcg_context *ctx, mcg_particle *d_particles, int64_t n, int32_t *d_results,

@@ -35,6 +35,10 @@ __global__ void mcg_libm_eval_kernel(int fn, const float *in, float *out, int64_
       r = __log2f(v);
     else if (fn == 5)
       r = mcg_log2_flight(v);
+    else if (fn == 6)
+      /* the fast flight sample's log2 from the state's top 32 bits t,
+       * passed as the argument's bit pattern */
+      r = mcg_flight_log2((uint64_t)__float_as_uint(v) << 31);
     else if (fn == 3) {
       /* expf with the general path forced for every argument */
       float d = 0.5f;
@@ -68,7 +72,7 @@ extern "C" int mcg_rnd_real_device(mcg_context *ctx, uint64_t *d_seeds, float *d
 extern "C" int mcg_libm_eval_device(mcg_context *ctx, int fn, const float *d_in, float *d_out,
                                     int64_t n)
 {
-  if (!ctx || fn < 0 || fn > 5 || n < 0 || (n > 0 && (!d_in || !d_out)))
+  if (!ctx || fn < 0 || fn > 6 || n < 0 || (n > 0 && (!d_in || !d_out)))
     return mcg_fail(MCG_ERR_ARG, "mcg_libm_eval_device: bad arguments");
   if (!ctx->libm_loaded)
     return mcg_fail(MCG_ERR_STATE, "mcg_libm_eval_device: needs a strict context");
@@ -164,4 +168,76 @@ extern "C" int mcg_verify_division(mcg_context *ctx, int mode, uint64_t n, uint6
   *mismatches = h[1];
   *example = h[2];
   return MCG_OK;
+}
+
+/* Throughput of the int <-> float conversions the trackers use (testing
+ * aid for the roofline): every thread runs four independent dependency
+ * chains of `iters` conversions of one kind, each followed by one 32-bit
+ * logic operation that feeds the next conversion.  kind 0: u64 -> f32,
+ * 1: f32 -> s64, 2: u32 -> f32, 3: f32 -> u32 (round to nearest). */
+__global__ void mcg_conv_rate_kernel(int kind, int iters, unsigned long long *sink)
+{
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t u[4];
+  float f[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    u[j] = (0x9E3779B97F4A7C15ull * (t * 4u + j + 1)) >> 2;
+    f[j] = __uint_as_float(0x3f800000u | ((uint32_t)u[j] & 0x7fffffu)) * 1.0e6f;
+  }
+  if (kind == 0) {
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        u[j] ^= __float_as_uint(__ull2float_rn(u[j]));
+  } else if (kind == 1) {
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        f[j] = __uint_as_float(__float_as_uint(f[j]) ^ ((uint32_t)__float2ll_rn(f[j]) & 0x3ffu));
+  } else if (kind == 2) {
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        u[j] ^= __float_as_uint(__uint2float_rn((uint32_t)u[j]));
+  } else {
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        f[j] = __uint_as_float(__float_as_uint(f[j]) ^ (__float2uint_rn(f[j]) & 0x3ffu));
+  }
+  unsigned long long x = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    x ^= u[j] ^ __float_as_uint(f[j]);
+  if (x == 0x1234567ull) /* never in practice; keeps the chains live */
+    sink[0] = x;
+}
+
+extern "C" int mcg_measure_conversion_rates(mcg_context *ctx, double *h_rates)
+{
+  if (!ctx || !h_rates)
+    return mcg_fail(MCG_ERR_ARG, "mcg_measure_conversion_rates: bad arguments");
+  cudaSetDevice(ctx->device);
+  unsigned long long *d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(unsigned long long));
+  if (e != cudaSuccess)
+    return mcg_cuda_fail(e, "cudaMalloc(conversion rates)");
+  const int grid = ctx->sm_count * 8, block = 256, iters = 2048;
+  for (int kind = 0; kind < 4 && e == cudaSuccess; ++kind) {
+    float ms = 0.f;
+    for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) { /* warm-up, then timed */
+      cudaEventRecord(ctx->ev0, ctx->stream);
+      mcg_conv_rate_kernel<<<grid, block, 0, ctx->stream>>>(kind, iters, d);
+      e = cudaGetLastError();
+      cudaEventRecord(ctx->ev1, ctx->stream);
+      if (e == cudaSuccess)
+        e = cudaStreamSynchronize(ctx->stream);
+      if (e == cudaSuccess)
+        e = cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    }
+    h_rates[kind] = (double)grid * block * iters * 4 / (ms * 1e-3);
+  }
+  cudaFree(d);
+  return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(e, "mcg_measure_conversion_rates");
 }

@@ -21,6 +21,7 @@
  */
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 #include <vector>
 
@@ -37,27 +38,21 @@
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[MCG_NOALLOC_BYTES];
 
-/* Device address of g_noalloc_scratch, looked up once per device with that
- * device current: in host code the symbol names a host-side stand-in, not
- * device memory. */
-static std::mutex g_noalloc_mu;
-static std::vector<unsigned char *> g_noalloc_addr;
 /* Serialises whole calls (the scratch array is shared). */
 static std::mutex g_noalloc_call_mu;
 
-static int noalloc_scratch(int device, unsigned char **out)
+/* Device address of g_noalloc_scratch in the current device's context.  In
+ * host code the symbol names a host-side stand-in, not device memory, so the
+ * address is looked up with the device current, on every call: a caller that
+ * resets the device (cudaDeviceReset) or otherwise recreates its context gets
+ * the new context's copy of the array, never a stale address. */
+static int noalloc_scratch(unsigned char **out)
 {
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if ((int)g_noalloc_addr.size() <= device)
-    g_noalloc_addr.resize(device + 1, nullptr);
-  if (!g_noalloc_addr[device]) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess)
-      return mcg_cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
-    g_noalloc_addr[device] = static_cast<unsigned char *>(p);
-  }
-  *out = g_noalloc_addr[device];
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess)
+    return mcg_cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
+  *out = static_cast<unsigned char *>(p);
   return MCG_OK;
 }
 
@@ -71,23 +66,29 @@ extern "C" int mcg_simulate_fast_noalloc(int n_layers, const int32_t *h_index_st
   if (n_layers <= 0 || !h_index_start || !h_m || !h_dx || !h_sigs || !h_rates || n < 0 ||
       (n > 0 && !d_particles) || !d_tally_q || log2_scale < 0 || log2_scale > 62)
     return mcg_fail(MCG_ERR_ARG, "mcg_simulate_fast_noalloc: bad arguments");
-  int total = 0;
+  /* the running total is checked against the limit at every layer, so it
+   * never grows past MCG_NOALLOC_MAX_CELLS + INT32_MAX (held in 64 bits) */
+  int64_t total64 = 0;
   for (int l = 0; l < n_layers; ++l) {
-    if (h_m[l] <= 0 || (l > 0 && h_index_start[l] != h_index_start[l - 1] + h_m[l - 1]))
+    if (h_m[l] <= 0 || (l > 0 && (int64_t)h_index_start[l] !=
+                                     (int64_t)h_index_start[l - 1] + h_m[l - 1]))
       return mcg_fail(MCG_ERR_ARG, "mcg_simulate_fast_noalloc: layer %d is empty or not contiguous", l);
-    total += h_m[l];
+    total64 += h_m[l];
+    if (total64 > MCG_NOALLOC_MAX_CELLS)
+      return mcg_fail(MCG_ERR_ARG,
+                      "mcg_simulate_fast_noalloc: chain of more than %d cells exceeds the fixed "
+                      "scratch (at most %d cells)", MCG_NOALLOC_MAX_CELLS, MCG_NOALLOC_MAX_CELLS);
   }
-  if (total > MCG_NOALLOC_MAX_CELLS)
-    return mcg_fail(MCG_ERR_ARG,
-                    "mcg_simulate_fast_noalloc: chain of %d cells exceeds the fixed scratch "
-                    "(at most %d cells)", total, MCG_NOALLOC_MAX_CELLS);
+  const int total = (int)total64;
+  if (n > 0 && (reinterpret_cast<uintptr_t>(d_particles) & 7u))
+    return mcg_fail(MCG_ERR_ARG, "mcg_simulate_fast_noalloc: d_particles must be 8-byte aligned");
   std::lock_guard<std::mutex> call_lock(g_noalloc_call_mu);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess)
     return mcg_cuda_fail(e, "cudaGetDevice");
   unsigned char *base = nullptr;
-  int rc = noalloc_scratch(dev, &base);
+  int rc = noalloc_scratch(&base);
   if (rc != MCG_OK)
     return rc;
   float4 *cells = reinterpret_cast<float4 *>(base + MCG_NOALLOC_CELLS_OFF);
@@ -129,12 +130,21 @@ extern "C" int mcg_simulate_fast_noalloc(int n_layers, const int32_t *h_index_st
     const int warps = block / 32;
     const int copies = ((size_t)total * 8 * warps <= 24 * 1024) ? warps : 1;
     P.tally_copies = copies;
-    const size_t smem = sizeof(mcg_libm_tab) + 16 * sizeof(unsigned long long) +
-                        (size_t)total * 8 * copies;
-    auto kern = mcg_track_kernel<false, MCG_TALLY_SMEM32>;
-    int sms = 0, bps = 0;
+    const size_t base_smem = sizeof(mcg_libm_tab) + 16 * sizeof(unsigned long long);
+    int sms = 0, optin = 0, bps = 0;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess)
+      return mcg_cuda_fail(e, "mcg_simulate_fast_noalloc: device attributes");
+    /* as the context path: a chain whose tally does not fit in the block's
+     * shared memory adds its deposits to the scratch tally directly */
+    const bool smem_tally = base_smem + (size_t)total * 8 * copies <= (size_t)optin;
+    const size_t smem = base_smem + (smem_tally ? (size_t)total * 8 * copies : 0);
+    auto kern = smem_tally ? mcg_track_kernel<false, MCG_TALLY_SMEM32, false>
+                           : mcg_track_kernel<false, MCG_TALLY_GLOBAL, false>;
+    /* the attribute is raised to the device's limit (the same value every
+     * caller of this library sets), so a concurrent launch of the same kernel
+     * from another host thread can never lower it below this launch's need */
+    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin)) != cudaSuccess ||
         (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, block, smem)) != cudaSuccess)
       return mcg_cuda_fail(e, "mcg_simulate_fast_noalloc: launch set-up");
     long long want = (n + block - 1) / block;

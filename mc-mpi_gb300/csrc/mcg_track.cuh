@@ -68,6 +68,38 @@ __device__ __forceinline__ void mcg_tally_add(unsigned long long *t, long long q
   }
 }
 
+/* Adds the fixed-point deposit llrint(dw 2^S) (ties to even, the oracle's
+ * quantisation) to a tally cell.  A deposit with 0 <= dw 2^S < 2^31 (all but
+ * the largest, and the negative ones of particles started outside their
+ * cell) converts with the 32-bit conversion and adds with one 32-bit atomic
+ * and a carry into the high word; the others take the 64-bit conversion,
+ * which issues on the FP64 pipe (about 6e11/s per GB300, the strict
+ * tracker's binding resource while it ran on every step). */
+template <int TALLY>
+__device__ __forceinline__ void mcg_deposit_u31(unsigned long long *t, float v)
+{
+  /* v = dw 2^S with +0 <= v < 2^31: the 32-bit conversion is exact */
+  const uint32_t q = __float2uint_rn(v);
+  if (TALLY == MCG_TALLY_SMEM32) {
+    unsigned *w = reinterpret_cast<unsigned *>(t);
+    const uint32_t old = atomicAdd(w, q);
+    if ((uint32_t)(old + q) < old)
+      atomicAdd(w + 1, 1u);
+  } else {
+    atomicAdd(t, (unsigned long long)q);
+  }
+}
+
+template <int TALLY>
+__device__ __forceinline__ void mcg_deposit(unsigned long long *t, float dw, int S)
+{
+  const float v = __fmul_rn(dw, mcg_fixed_scale(S));
+  if (__float_as_uint(v) < 0x4f000000u) /* +0 <= v < 2^31 */
+    mcg_deposit_u31<TALLY>(t, v);
+  else
+    mcg_tally_add<TALLY>(t, mcg_to_fixed(dw, S));
+}
+
 enum { MCG_CNT_HIST = 0, MCG_CNT_STEPS, MCG_CNT_SCAT, MCG_CNT_LEFT, MCG_CNT_RIGHT, MCG_CNT_KILL,
        MCG_CNT_WLEFT, MCG_CNT_WRIGHT, MCG_CNT_WKILL, MCG_CNT_ERR, MCG_CNT_N };
 
@@ -111,8 +143,11 @@ __device__ __forceinline__ void mcg_load_particle(const mcg_track_params &P, int
  * *tally_cell.  STRICT: the reference's float operations and host-libm
  * logf/expf; the crossing's absorption is computed before the logarithm and
  * a certified exponential bound settles most crossings without it (see
- * MCG_CROSS_FACTOR).  FAST: hardware log2/exp2. */
-template <bool STRICT, int TALLY>
+ * mcg_cross_threshold).  FAST: hardware log2/exp2.  THIN (strict; chains
+ * whose crossings almost all have |sig_a de| < MCG_EXP_SMALL_T): the
+ * certain-crossing path evaluates only the small-argument exp form and
+ * leaves the rarer larger arguments to the full step. */
+template <bool STRICT, int TALLY, bool THIN = false>
 __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, float &wmc,
                                          float &inv_mu, int &idx, uint32_t &nsc, const float4 c,
                                          unsigned long long *tally_cell, int qs,
@@ -121,35 +156,48 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
                                          bool *coll_out = nullptr, float *dep_out = nullptr)
 {
   const float sig_a = c.x;
-  const float h = STRICT ? mcg_rnd_real(seed) : mcg_rnd_real_fast(seed);
+  mcg_lcg_next(seed); /* the flight sample's state */
   const bool neg = mu < 0.0f;
   int inew = neg ? idx - 1 : idx + 1;
   const float edge = neg ? c.z : c.w;
   float om;
   if (STRICT) {
     /* The certain crossing, computed without branches: d_edge by the cached
-     * reciprocal, the crossing's absorption by the exp evaluator, and the
-     * certified bound.  It is the reference's step exactly when every
-     * condition in `easy` holds (division and exp arguments in the range
-     * where those forms are exact, no exception-table candidate, a flight
-     * certainly past the edge); almost every step of a fine mesh is such a
-     * crossing.  Any other step takes the full step below with the same h. */
+     * reciprocal, the crossing's absorption by the exp evaluator, its
+     * deposit, and the certified bound.  It is the reference's step exactly
+     * when every condition in `easy` holds (division and exp arguments in the
+     * range where those forms are exact, no exception-table candidate, a
+     * deposit below 2^31 fixed-point units, a flight certainly past the
+     * edge); almost every step of a fine mesh is such a crossing.  Any other
+     * step takes the full step below with the same state. */
     const float a = __fsub_rn(edge, x), aa = fabsf(a);
     const float de_q = mcg_div_by_rcp(a, mu, inv_mu);
     const float t_q = __fmul_rn(-sig_a, de_q);
     float d_q;
-    const float y_q = mcg_exp_ff_core(t_q, &d_q, T);
-    const float bound_q = __fmul_rn(
-        mcg_ex2_approx(__fmul_rn(__fmul_rn(c.y, de_q), -MCG_LOG2E_F)), MCG_CROSS_FACTOR);
-    const bool easy = (inv_mu != 0.0f) & (aa >= 0x1p-100f) & (aa <= 0x1p100f) &
-                      (t_q >= MCG_EXP_ONE_BOUND) & (t_q < 89.0f) & (d_q > LM.tau_exp_max) &
-                      (c.y > MCG_EPS) & (h < bound_q);
-    bool cross = true;
-    float de = de_q, di = MCG_MAXREAL;
+    const float y_q = THIN ? mcg_exp_ff_small(t_q, &d_q) : mcg_exp_ff_core(t_q, &d_q, T);
+    const float dw_q = __fmul_rn(__fsub_rn(1.0f, y_q), wmc);
+    const float v_q = __fmul_rn(dw_q, mcg_fixed_scale(qs));
+    const bool t_ok = THIN ? (fabsf(t_q) < MCG_EXP_SMALL_T)
+                           : ((t_q >= MCG_EXP_ONE_BOUND) & (t_q < 89.0f));
+    const bool easy = (inv_mu != 0.0f) & (aa >= 0x1p-100f) & (aa <= 0x1p100f) & t_ok &
+                      (d_q > LM.tau_exp_max) & (__float_as_uint(v_q) < 0x4f000000u) &
+                      (mcg_state_hi(seed) < mcg_cross_threshold(c.y, de_q));
     if (easy) {
       x = edge;
-      om = __fsub_rn(1.0f, y_q);
-    } else {
+      wmc = __fsub_rn(wmc, dw_q);
+      if (tally_cell)
+        mcg_deposit_u31<TALLY>(tally_cell, v_q);
+      if (l_out) {
+        *l_out = de_q;
+        *coll_out = false;
+        *dep_out = dw_q;
+      }
+      idx = inew;
+      return;
+    }
+    bool cross = true;
+    float de, di = MCG_MAXREAL;
+    {
       /* d_edge, and the crossing's absorption, do not depend on the flight
        * sample: start them before the logarithm */
       de = inv_mu == 0.0f ? MCG_MAXREAL
@@ -158,12 +206,10 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
       const float om_cross = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, de), T, LM);
       /* di = sig_i > EPS ? -log(h) / sig_i : MAXREAL; the exact value is
        * only needed when the flight may end inside the cell: the certified
-       * test h < ~exp(-sig_i de) settles almost every crossing */
+       * test settles almost every crossing */
       if (c.y > MCG_EPS) {
-        const float bound = __fmul_rn(
-            mcg_ex2_approx(__fmul_rn(__fmul_rn(c.y, de), -MCG_LOG2E_F)), MCG_CROSS_FACTOR);
-        if (!(h < bound)) {
-          di = __fdiv_rn(-mcg_logf_strict(h, T, LM), c.y);
+        if (!(mcg_state_hi(seed) < mcg_cross_threshold(c.y, de))) {
+          di = __fdiv_rn(-mcg_logf_strict(mcg_unit_of(seed), T, LM), c.y);
           cross = !(di < de);
         }
       } else {
@@ -184,7 +230,7 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
     const float dw = __fmul_rn(om, wmc);
     wmc = __fsub_rn(wmc, dw);
     if (tally_cell)
-      mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dw, qs));
+      mcg_deposit<TALLY>(tally_cell, dw, qs);
     if (l_out) {
       *l_out = cross ? de : di;
       *coll_out = !cross;
@@ -193,7 +239,7 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
   } else {
     const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
     const float om_cross = mcg_one_minus_exp_fast(-sig_a * de);
-    const float di = c.y != 0.0f ? mcg_log2_flight(h) * c.y : MCG_MAXREAL;
+    const float di = c.y != 0.0f ? mcg_flight_log2(seed) * c.y : MCG_MAXREAL;
     const bool coll = di < de;
     if (l_out) {
       *l_out = coll ? di : de;
@@ -217,7 +263,7 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
     const float dep = __fsub_rn(wmc, wnew);
     wmc = wnew;
     if (tally_cell)
-      mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dep, qs));
+      mcg_deposit<TALLY>(tally_cell, dep, qs);
     if (dep_out)
       *dep_out = dep;
   }
@@ -226,11 +272,12 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
 
 /* One Layer::particle_step (src/layer.cpp:123-190) on a lane's particle in
  * cell c = {sig_a, sig_i or -ln2/sig_i, edge_lo, edge_hi}, in two parts, for
- * the event-based tracker: mcg_step_cross draws the flight sample h and
- * completes the step when it is a certain crossing (STRICT: the branch-free
- * path of mcg_step; FAST: the flight ends past the edge), returning true;
- * otherwise it changes nothing but the seed and returns false, and
- * mcg_step_rest completes the step from h.  Together they perform exactly
+ * the event-based tracker: mcg_step_cross advances the state to the flight
+ * sample's and completes the step when it is a certain crossing (STRICT: the
+ * branch-free path of mcg_step; FAST: the flight ends past the edge),
+ * returning true; otherwise it changes nothing but the seed and returns
+ * false, and mcg_step_rest completes the step from the advanced state, which
+ * determines the flight sample.  Together they perform exactly
  * mcg_step's operations (mcg_step, the one-piece form above, serves the
  * history-based kernels, where the split costs about 6 %).  STRICT: the reference's float operations and host-libm
  * logf/expf; the crossing's absorption is computed before the logarithm and
@@ -243,11 +290,11 @@ __device__ __forceinline__ bool mcg_step_cross(uint64_t &seed, float &x, float &
                                                float &inv_mu, int &idx, const float4 c,
                                                unsigned long long *tally_cell, int qs,
                                                const mcg_libm_tab *T, const mcg_libm_dev &LM,
-                                               float &h, float *l_out = nullptr,
+                                               float *l_out = nullptr,
                                                bool *coll_out = nullptr, float *dep_out = nullptr)
 {
   const float sig_a = c.x;
-  h = STRICT ? mcg_rnd_real(seed) : mcg_rnd_real_fast(seed);
+  mcg_lcg_next(seed); /* the flight sample's state */
   const bool neg = mu < 0.0f;
   const float edge = neg ? c.z : c.w;
   if (STRICT) {
@@ -263,18 +310,16 @@ __device__ __forceinline__ bool mcg_step_cross(uint64_t &seed, float &x, float &
     const float t_q = __fmul_rn(-sig_a, de_q);
     float d_q;
     const float y_q = mcg_exp_ff_core(t_q, &d_q, T);
-    const float bound_q = __fmul_rn(
-        mcg_ex2_approx(__fmul_rn(__fmul_rn(c.y, de_q), -MCG_LOG2E_F)), MCG_CROSS_FACTOR);
     const bool easy = (inv_mu != 0.0f) & (aa >= 0x1p-100f) & (aa <= 0x1p100f) &
                       (t_q >= MCG_EXP_ONE_BOUND) & (t_q < 89.0f) & (d_q > LM.tau_exp_max) &
-                      (c.y > MCG_EPS) & (h < bound_q);
+                      (mcg_state_hi(seed) < mcg_cross_threshold(c.y, de_q));
     if (!easy)
       return false;
     x = edge;
     const float dw = __fmul_rn(__fsub_rn(1.0f, y_q), wmc);
     wmc = __fsub_rn(wmc, dw);
     if (tally_cell)
-      mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dw, qs));
+      mcg_deposit<TALLY>(tally_cell, dw, qs);
     if (l_out) {
       *l_out = de_q;
       *coll_out = false;
@@ -282,7 +327,7 @@ __device__ __forceinline__ bool mcg_step_cross(uint64_t &seed, float &x, float &
     }
   } else {
     const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
-    const float di = c.y != 0.0f ? mcg_log2_flight(h) * c.y : MCG_MAXREAL;
+    const float di = c.y != 0.0f ? mcg_flight_log2(seed) * c.y : MCG_MAXREAL;
     if (di < de)
       return false;
     if (l_out) {
@@ -298,7 +343,7 @@ __device__ __forceinline__ bool mcg_step_cross(uint64_t &seed, float &x, float &
     const float dep = __fsub_rn(wmc, wnew);
     wmc = wnew;
     if (tally_cell)
-      mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dep, qs));
+      mcg_deposit<TALLY>(tally_cell, dep, qs);
     if (dep_out)
       *dep_out = dep;
   }
@@ -307,7 +352,7 @@ __device__ __forceinline__ bool mcg_step_cross(uint64_t &seed, float &x, float &
 }
 
 template <bool STRICT, int TALLY>
-__device__ __forceinline__ void mcg_step_rest(float h, uint64_t &seed, float &x, float &mu,
+__device__ __forceinline__ void mcg_step_rest(uint64_t &seed, float &x, float &mu,
                                               float &wmc, float &inv_mu, int &idx, uint32_t &nsc,
                                               const float4 c, unsigned long long *tally_cell,
                                               int qs, const mcg_libm_tab *T,
@@ -329,14 +374,12 @@ __device__ __forceinline__ void mcg_step_rest(float h, uint64_t &seed, float &x,
     const float om_cross = mcg_one_minus_expf_strict(__fmul_rn(-sig_a, de), T, LM);
     /* di = sig_i > EPS ? -log(h) / sig_i : MAXREAL; the exact value is
      * only needed when the flight may end inside the cell: the certified
-     * test h < ~exp(-sig_i de) settles almost every crossing */
+     * test settles almost every crossing */
     bool cross = true;
     float di = MCG_MAXREAL;
     if (c.y > MCG_EPS) {
-      const float bound = __fmul_rn(
-          mcg_ex2_approx(__fmul_rn(__fmul_rn(c.y, de), -MCG_LOG2E_F)), MCG_CROSS_FACTOR);
-      if (!(h < bound)) {
-        di = __fdiv_rn(-mcg_logf_strict(h, T, LM), c.y);
+      if (!(mcg_state_hi(seed) < mcg_cross_threshold(c.y, de))) {
+        di = __fdiv_rn(-mcg_logf_strict(mcg_unit_of(seed), T, LM), c.y);
         cross = !(di < de);
       }
     } else {
@@ -356,7 +399,7 @@ __device__ __forceinline__ void mcg_step_rest(float h, uint64_t &seed, float &x,
     const float dw = __fmul_rn(om, wmc);
     wmc = __fsub_rn(wmc, dw);
     if (tally_cell)
-      mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dw, qs));
+      mcg_deposit<TALLY>(tally_cell, dw, qs);
     if (l_out) {
       *l_out = cross ? de : di;
       *coll_out = !cross;
@@ -365,7 +408,7 @@ __device__ __forceinline__ void mcg_step_rest(float h, uint64_t &seed, float &x,
   } else {
     const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
     const float om_cross = mcg_one_minus_exp_fast(-sig_a * de);
-    const float di = c.y != 0.0f ? mcg_log2_flight(h) * c.y : MCG_MAXREAL;
+    const float di = c.y != 0.0f ? mcg_flight_log2(seed) * c.y : MCG_MAXREAL;
     const bool coll = di < de;
     if (l_out) {
       *l_out = coll ? di : de;
@@ -386,14 +429,14 @@ __device__ __forceinline__ void mcg_step_rest(float h, uint64_t &seed, float &x,
     const float dep = __fsub_rn(wmc, wnew);
     wmc = wnew;
     if (tally_cell)
-      mcg_tally_add<TALLY>(tally_cell, mcg_to_fixed(dep, qs));
+      mcg_deposit<TALLY>(tally_cell, dep, qs);
     if (dep_out)
       *dep_out = dep;
   }
   idx = inew;
 }
 
-template <bool STRICT, int TALLY>
+template <bool STRICT, int TALLY, bool THIN>
 __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -475,15 +518,12 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
        * range test of simulate_particle's loop */
       const int kmax = (int)min((uint32_t)P.refill_steps, P.max_steps - nst);
       int k = 0;
-      bool going = true;
-      for (; k < kmax; ++k) {
-        if (!((wmc >= min_w) & ((unsigned)idx < (unsigned)ncell))) {
-          going = false;
-          break;
-        }
-        mcg_step<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + idx),
-                                &my_tally[idx], qs, T, P.libm);
+      while ((k < kmax) & (wmc >= min_w) & ((unsigned)idx < (unsigned)ncell)) {
+        mcg_step<STRICT, TALLY, THIN>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + idx),
+                                      &my_tally[idx], qs, T, P.libm);
+        ++k;
       }
+      const bool going = (wmc >= min_w) & ((unsigned)idx < (unsigned)ncell);
       nst += (uint32_t)k;
       if (!going || nst >= P.max_steps) {
         /* history ends: classification of simulate_particle; a history

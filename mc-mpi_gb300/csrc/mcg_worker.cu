@@ -267,6 +267,31 @@ __global__ void __launch_bounds__(1024) mcg_worker_cycle(mcg_worker_params P)
   }
 }
 
+static size_t worker_align(size_t b)
+{
+  return (b + 255) & ~(size_t)255;
+}
+
+/* The context's worker buffer, at least `bytes` long. */
+static int worker_buffer(mcg_context *ctx, size_t bytes, unsigned char **out)
+{
+  if (!ctx->ext)
+    ctx->ext = new mcg_ext();
+  mcg_worker_state &W = ctx->ext->worker;
+  if (W.bytes < bytes) {
+    if (W.dev)
+      cudaFree(W.dev);
+    W.dev = nullptr;
+    W.bytes = 0;
+    cudaError_t e = cudaMalloc(&W.dev, bytes);
+    if (e != cudaSuccess)
+      return mcg_cuda_fail(e, "workers: cudaMalloc(queues)");
+    W.bytes = bytes;
+  }
+  *out = static_cast<unsigned char *>(W.dev);
+  return MCG_OK;
+}
+
 extern "C" int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n,
                               int32_t per_cycle, int64_t queue_capacity, int64_t *h_cycles,
                               int64_t *h_handoffs)
@@ -298,20 +323,21 @@ extern "C" int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n
   const size_t smem_base = sizeof(mcg_libm_tab) + 4 * sizeof(unsigned long long);
   const bool use_smem = smem_base + (size_t)ctx->n_cells * 8 <= (size_t)ctx->smem_optin;
   const size_t smem = smem_base + (use_smem ? (size_t)ctx->n_cells * 8 : 0);
-  /* device state: layers, queues, counters (freed at the end of the call) */
-  void *d_lay = nullptr, *d_q = nullptr, *d_c = nullptr;
+  /* device state: layers, queues, counters, in the context's worker
+   * buffer (allocated once, grown when a call needs more) */
+  const size_t o_lay = 0, o_c = worker_align(P_ * sizeof(mcg_worker_layer));
+  const size_t o_q = o_c + 256;
+  unsigned char *wb = nullptr;
+  int rcb = worker_buffer(ctx, o_q + (size_t)P_ * queue_capacity * sizeof(mcg_particle), &wb);
+  if (rcb != MCG_OK)
+    return rcb;
+  void *d_lay = wb + o_lay, *d_q = wb + o_q, *d_c = wb + o_c;
   cudaError_t e;
-  if ((e = cudaMalloc(&d_lay, P_ * sizeof(mcg_worker_layer))) != cudaSuccess ||
-      (e = cudaMalloc(&d_q, (size_t)P_ * queue_capacity * sizeof(mcg_particle))) != cudaSuccess ||
-      (e = cudaMalloc(&d_c, 64)) != cudaSuccess) {
-    cudaFree(d_lay);
-    cudaFree(d_q);
-    return mcg_cuda_fail(e, "mcg_worker_run: cudaMalloc");
-  }
   /* src_next, done, handoffs, cycles with work, items of the cycle, first newborn of it */
   unsigned long long *cnt = static_cast<unsigned long long *>(d_c);
-  cudaMemcpy(d_lay, lay.data(), P_ * sizeof(mcg_worker_layer), cudaMemcpyHostToDevice);
-  cudaMemset(d_c, 0, 64);
+  if ((e = cudaMemcpy(d_lay, lay.data(), P_ * sizeof(mcg_worker_layer), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemset(d_c, 0, 64)) != cudaSuccess)
+    return mcg_cuda_fail(e, "mcg_worker_run: set-up");
   mcg_worker_params W;
   memset(&W, 0, sizeof(W));
   W.cells = strict ? ctx->d_cells_strict : ctx->d_cells_fast;
@@ -340,12 +366,20 @@ extern "C" int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n
   W.max_steps = ctx->max_steps;
   auto kern = strict ? (use_smem ? mcg_worker_cycle<true, true> : mcg_worker_cycle<true, false>)
                      : (use_smem ? mcg_worker_cycle<false, true> : mcg_worker_cycle<false, false>);
-  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin);
   int bps = 1;
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 1024, smem);
   const int grid = ctx->sm_count * std::max(bps, 1);
   int64_t cycles = 0;
+  /* Termination bound: every cycle with work takes at least one step of some
+   * history, and every history ends within max_steps steps of each of its
+   * visits to a sub-domain, one visit per hand-over, so the loop needs at
+   * most n * max_steps cycles with work; a check every 8 cycles that finds
+   * no work while histories are unfinished is an inconsistency, reported as
+   * MCG_ERR_STATE rather than looped on. */
+  const double max_cycles = (double)std::max<int64_t>(n, 1) * (double)ctx->max_steps + 8.0;
+  unsigned long long last_work_cycles = 0;
   unsigned long long host[4] = {0, 0, 0, 0}; /* src_next, done, handoffs, cycles with work */
   int rc = MCG_OK;
   cudaEventRecord(ctx->ev0, ctx->stream);
@@ -371,17 +405,20 @@ extern "C" int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n
     }
     if (host[1] >= (unsigned long long)n)
       break;
-    if (cycles > (int64_t)1 << 40) {
-      rc = mcg_fail(MCG_ERR_LIMIT, "mcg_worker_run: no termination");
+    if (host[3] == last_work_cycles) {
+      rc = mcg_fail(MCG_ERR_STATE, "mcg_worker_run: %llu of %lld histories finished and no "
+                    "particle left to simulate", host[1], (long long)n);
+      break;
+    }
+    last_work_cycles = host[3];
+    if ((double)cycles > max_cycles) {
+      rc = mcg_fail(MCG_ERR_LIMIT, "mcg_worker_run: more cycles than n * max_steps");
       break;
     }
   }
   cudaEventRecord(ctx->ev1, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
   cudaEventElapsedTime(&ctx->last_ms, ctx->ev0, ctx->ev1);
-  cudaFree(d_lay);
-  cudaFree(d_q);
-  cudaFree(d_c);
   if (e != cudaSuccess)
     return mcg_cuda_fail(e, "mcg_worker_run");
   if (rc != MCG_OK)
@@ -391,6 +428,404 @@ extern "C" int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n
   cudaMemcpy(ctx->d_counters + MCG_CNT_HIST, &hcount, 8, cudaMemcpyHostToDevice);
   if (h_cycles)
     *h_cycles = (int64_t)host[3]; /* launched cycles past the last one with work ran empty */
+  if (h_handoffs)
+    *h_handoffs = (int64_t)host[2];
+  return MCG_OK;
+}
+
+/* ---------------------------------------------------------------------------
+ * The asynchronous form (WorkerAsync / WorkerRma, src/worker_async.cpp:19-105,
+ * src/async_comm.cpp, src/rma_comm.cpp): no cycles.  One persistent launch;
+ * every warp takes work for its idle lanes from any sub-domain's queue (or
+ * newborns from the source), simulates each particle inside its sub-domain
+ * and appends leavers to the neighbour's queue, until the device counter of
+ * finished histories reaches N.  The queues are bounded multi-producer
+ * multi-consumer rings with a publication word per slot: slot s of a ring
+ * of capacity C is free for ticket t when seq[s] == t and holds ticket t
+ * when seq[s] == t + 1; a producer takes a ticket with one atomic and
+ * writes the particle and then seq = t + 1, a consumer claims a run of
+ * published tickets with one compare-and-swap on the ring's head and, after
+ * reading, frees the slots for the next lap (seq = t + C).  Nothing waits on
+ * a slot: a producer that finds its slot still occupied (the ring holds C
+ * particles) sets the overflow flag, as the reference aborts on a full
+ * buffer.  Warps without work sleep briefly and poll; they give up with
+ * MCG_ERR_TIMEOUT after `idle_limit_ns` without any history finishing.
+ * Every particle follows the trajectory of the fused tracker, so the tally
+ * equals it.
+ * ------------------------------------------------------------------------- */
+struct mcg_aq_ring {
+  int32_t lo, hi;           /* cell range of the sub-domain (global indices) */
+  unsigned long long enq;   /* tickets handed to producers */
+  unsigned long long deq;   /* tickets claimed by consumers */
+  unsigned long long pad[5];
+};
+
+struct mcg_async_params {
+  const float4 *cells;
+  int32_t n_layers, cell_lo, n_cells, src_layer;
+  mcg_aq_ring *rings;
+  mcg_particle *slots;          /* n_layers x cap */
+  unsigned long long *seq;      /* n_layers x cap publication words */
+  unsigned long long cap;
+  mcg_source src;
+  unsigned long long *src_next; /* newborns handed out so far */
+  unsigned long long src_total;
+  int32_t refill_steps;
+  float min_w;
+  int32_t q_log2;
+  unsigned long long *tally, *counters, *done, *handoffs;
+  mcg_libm_dev libm;
+  const mcg_libm_tab *libm_tab;
+  uint32_t max_steps;
+  unsigned long long idle_limit_ns;
+};
+
+__device__ __forceinline__ unsigned long long mcg_ld_acquire(const unsigned long long *p)
+{
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void mcg_st_release(unsigned long long *p, unsigned long long v)
+{
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long mcg_globaltimer()
+{
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+template <bool STRICT, bool SMEM>
+__global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  mcg_libm_tab *T = reinterpret_cast<mcg_libm_tab *>(smem);
+  int2 *s_rng = reinterpret_cast<int2 *>(smem + sizeof(mcg_libm_tab)); /* [n_layers] lo, hi local */
+  unsigned long long *s_tally =
+      reinterpret_cast<unsigned long long *>(s_rng + ((P.n_layers + 1) & ~1));
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int gwarp = (int)((blockIdx.x * blockDim.x + tid) >> 5);
+  if (STRICT)
+    for (int i = tid; i < (int)(sizeof(mcg_libm_tab) / 4); i += blockDim.x)
+      reinterpret_cast<float *>(T)[i] = reinterpret_cast<const float *>(P.libm_tab)[i];
+  for (int l = tid; l < P.n_layers; l += blockDim.x)
+    s_rng[l] = make_int2(P.rings[l].lo - P.cell_lo, P.rings[l].hi - P.cell_lo);
+  if (SMEM)
+    for (int i = tid; i < P.n_cells; i += blockDim.x)
+      s_tally[i] = 0ull;
+  __syncthreads();
+  unsigned long long *tally = SMEM ? s_tally : P.tally;
+  const float min_w = P.min_w;
+  const int qs = P.q_log2;
+  const unsigned long long cap = P.cap;
+
+  uint64_t seed = 0;
+  float x = 0.f, mu = 0.f, wmc = 0.f, inv_mu = 0.f;
+  int idx = 0, L = 0, llo = 0, lhi = 0;
+  uint32_t nst = 0, nsc = 0;
+  bool active = false;
+  unsigned long long n_done = 0, n_hand = 0, steps = 0, scat = 0;
+  unsigned long long seen_done = 0, seen_t = 0;
+  int scan = gwarp % P.n_layers;
+  bool timed_out = false;
+
+  for (;;) {
+    unsigned need = __ballot_sync(0xffffffffu, !active);
+    if (need) {
+      /* 1. queued particles: scan the rings from this warp's rotating start
+       * and claim a run of published tickets of the first ring that has some */
+      for (int probe = 0; probe < P.n_layers && need; ++probe) {
+        const int l = (scan + probe) % P.n_layers;
+        mcg_aq_ring *R = &P.rings[l];
+        unsigned long long h = 0, e = 0;
+        if (lane == 0) {
+          h = *(volatile unsigned long long *)&R->deq;
+          e = *(volatile unsigned long long *)&R->enq;
+        }
+        h = __shfl_sync(0xffffffffu, h, 0);
+        e = __shfl_sync(0xffffffffu, e, 0);
+        if (e <= h)
+          continue;
+        const int cnt = __popc(need);
+        const unsigned long long want = min((unsigned long long)cnt, e - h);
+        const bool pub = (unsigned long long)lane < want &&
+                         mcg_ld_acquire(&P.seq[(size_t)l * cap + (h + lane) % cap]) == h + lane + 1;
+        const unsigned pubmask = __ballot_sync(0xffffffffu, pub);
+        /* leading published tickets */
+        const int m = pubmask == 0xffffffffu ? 32 : __ffs(~pubmask) - 1;
+        if (m <= 0)
+          continue;
+        unsigned long long got = 0;
+        if (lane == 0)
+          got = atomicCAS(&R->deq, h, h + (unsigned long long)m);
+        got = __shfl_sync(0xffffffffu, got, 0);
+        if (got != h)
+          continue; /* another warp claimed first: look again later */
+        __syncwarp();
+        const int rank = __popc(need & lanemask_lt());
+        if ((need >> lane) & 1u && rank < m) {
+          const unsigned long long t = h + rank;
+          const size_t s = (size_t)l * cap + t % cap;
+          /* the reading lane acquires the publication itself (another lane
+           * of the warp saw it, so this returns at once) */
+          int tries = 0;
+          while (mcg_ld_acquire(&P.seq[s]) != t + 1 && ++tries < (1 << 20))
+            ;
+          if (tries >= (1 << 20))
+            atomicOr(&P.counters[MCG_CNT_ERR], 4ull);
+          const mcg_particle q = P.slots[s];
+          mcg_st_release(&P.seq[s], t + cap); /* free for the next lap */
+          seed = q.seed, x = q.x, mu = q.mu, wmc = q.wmc, idx = q.index - P.cell_lo;
+          L = l;
+          llo = s_rng[l].x;
+          lhi = s_rng[l].y;
+          inv_mu = mcg_flight_rcp(mu);
+          nst = nsc = 0;
+          active = true;
+        }
+        need = __ballot_sync(0xffffffffu, !active);
+      }
+      /* 2. newborns from the source for the lanes still idle */
+      if (need && *(volatile unsigned long long *)P.src_next < P.src_total) {
+        const int cnt = __popc(need);
+        unsigned long long base = 0;
+        if (lane == 0)
+          base = atomicAdd(P.src_next, (unsigned long long)cnt);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const int rank = __popc(need & lanemask_lt());
+        if ((need >> lane) & 1u && base + rank < P.src_total) {
+          mcg_source_particle(P.src, (int64_t)(base + rank), seed, x, mu, wmc, idx);
+          idx -= P.cell_lo;
+          L = P.src_layer;
+          llo = s_rng[L].x;
+          lhi = s_rng[L].y;
+          inv_mu = mcg_flight_rcp(mu);
+          nst = nsc = 0;
+          active = true;
+        }
+      }
+      scan = (scan + 1) % P.n_layers;
+    }
+    if (!__any_sync(0xffffffffu, active)) {
+      /* nothing to do: finished, or wait for other warps' hand-overs */
+      unsigned long long d = 0;
+      if (lane == 0)
+        d = *(volatile unsigned long long *)P.done;
+      d = __shfl_sync(0xffffffffu, d, 0);
+      if (d >= P.src_total)
+        break;
+      if (*(volatile unsigned long long *)&P.counters[MCG_CNT_ERR] & 6ull)
+        break; /* a full ring, or a publication that never came */
+      const unsigned long long now = mcg_globaltimer();
+      if (d != seen_done || seen_t == 0) {
+        seen_done = d;
+        seen_t = now;
+      } else if (now - seen_t > P.idle_limit_ns) {
+        timed_out = true;
+        break;
+      }
+      __nanosleep(256);
+      continue;
+    }
+    int dir = 0;
+    bool finished = false;
+    if (active) {
+      const int kmax = (int)min((uint32_t)P.refill_steps, P.max_steps - nst);
+      int k = 0;
+      while ((k < kmax) & (wmc >= min_w) & ((unsigned)(idx - llo) < (unsigned)(lhi - llo))) {
+        mcg_step<STRICT, SMEM ? MCG_TALLY_SMEM32 : MCG_TALLY_GLOBAL>(
+            seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + idx), &tally[idx], qs, T, P.libm);
+        ++k;
+      }
+      nst += (uint32_t)k;
+      const bool going = (wmc >= min_w) & ((unsigned)(idx - llo) < (unsigned)(lhi - llo));
+      if (!going || nst >= P.max_steps) {
+        if (going)
+          atomicOr(&P.counters[MCG_CNT_ERR], 1ull); /* the step limit */
+        else if (idx == llo - 1)
+          dir = L == 0 ? 0 : -1; /* the chain's ends leak (src/layer.cpp:47-48) */
+        else if (idx == lhi)
+          dir = L == P.n_layers - 1 ? 0 : 1;
+        steps += nst;
+        scat += nsc;
+        finished = true;
+        active = false;
+      }
+    }
+    /* hand-over: one ticket atomic per destination ring and warp */
+    const unsigned movers = __ballot_sync(0xffffffffu, finished && dir != 0);
+    if (finished && dir == 0)
+      ++n_done;
+    if (finished && dir != 0) {
+      const int dst = L + dir;
+      const unsigned peers = __match_any_sync(movers, dst);
+      const int leader = __ffs(peers) - 1;
+      unsigned long long base = 0;
+      if (lane == leader)
+        base = atomicAdd(&P.rings[dst].enq, (unsigned long long)__popc(peers));
+      base = __shfl_sync(peers, base, leader);
+      const unsigned long long t = base + __popc(peers & lanemask_lt());
+      const size_t s = (size_t)dst * cap + t % cap;
+      if (mcg_ld_acquire(&P.seq[s]) != t) {
+        atomicOr(&P.counters[MCG_CNT_ERR], 2ull); /* the ring is full */
+      } else {
+        mcg_particle o;
+        o.seed = seed, o.x = x, o.mu = mu, o.wmc = wmc, o.index = idx + P.cell_lo;
+        P.slots[s] = o;
+        mcg_st_release(&P.seq[s], t + 1); /* publish */
+      }
+      ++n_hand;
+    }
+    /* finished histories count at once, so idle warps see progress */
+    unsigned long long fin = n_done;
+    for (int o = 16; o > 0; o >>= 1)
+      fin += __shfl_down_sync(0xffffffffu, fin, o);
+    if (lane == 0 && fin)
+      atomicAdd(P.done, fin);
+    n_done = 0;
+    /* a full ring ends the run for everyone */
+    if (*(volatile unsigned long long *)&P.counters[MCG_CNT_ERR] & 6ull)
+      break;
+  }
+  if (timed_out && lane == 0)
+    atomicOr(&P.counters[MCG_CNT_ERR], 4ull);
+  for (int o = 16; o > 0; o >>= 1) {
+    n_hand += __shfl_down_sync(0xffffffffu, n_hand, o);
+    steps += __shfl_down_sync(0xffffffffu, steps, o);
+    scat += __shfl_down_sync(0xffffffffu, scat, o);
+  }
+  if (lane == 0) {
+    if (n_hand)
+      atomicAdd(P.handoffs, n_hand);
+    atomicAdd(&P.counters[MCG_CNT_STEPS], steps);
+    atomicAdd(&P.counters[MCG_CNT_SCAT], scat);
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (int i = tid; i < P.n_cells; i += blockDim.x)
+      if (s_tally[i])
+        atomicAdd(&P.tally[i], s_tally[i]);
+  }
+}
+
+/* Every slot free for its first-lap ticket: seq[l * cap + s] = s. */
+__global__ void mcg_aq_init(unsigned long long *seq, unsigned long long total, unsigned long long cap)
+{
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < total;
+       i += (unsigned long long)gridDim.x * blockDim.x)
+    seq[i] = i % cap;
+}
+
+extern "C" int mcg_worker_run_async(mcg_context *ctx, const mcg_source *src, int64_t n,
+                                    int64_t queue_capacity, int64_t *h_handoffs)
+{
+  if (!ctx || !src || n < 0 || queue_capacity <= 0)
+    return mcg_fail(MCG_ERR_ARG, "mcg_worker_run_async: bad arguments");
+  if (!ctx->d_tally)
+    return mcg_fail(MCG_ERR_STATE, "mcg_worker_run_async: no layers set");
+  cudaSetDevice(ctx->device);
+  const bool strict = ctx->mode == MCG_MODE_STRICT;
+  if (strict && !ctx->libm_loaded) {
+    int rc = mcg_load_libm(ctx);
+    if (rc != MCG_OK)
+      return rc;
+  }
+  const int P_ = ctx->n_layers;
+  int src_layer = -1;
+  std::vector<mcg_aq_ring> rings(P_);
+  for (int l = 0; l < P_; ++l) {
+    memset(&rings[l], 0, sizeof(rings[l]));
+    rings[l].lo = ctx->layer_start[l];
+    rings[l].hi = ctx->layer_start[l] + ctx->layer_m[l];
+    if (src->cell0 >= rings[l].lo && src->cell0 < rings[l].hi)
+      src_layer = l;
+  }
+  if (src_layer < 0)
+    return mcg_fail(MCG_ERR_ARG, "mcg_worker_run_async: the source cell %d is outside the chain",
+                    src->cell0);
+  const unsigned long long cap = (unsigned long long)queue_capacity;
+  const size_t o_rings = 0, o_c = worker_align(P_ * sizeof(mcg_aq_ring));
+  const size_t o_seq = o_c + 256, o_slots = o_seq + worker_align((size_t)P_ * cap * 8);
+  unsigned char *wb = nullptr;
+  int rc = worker_buffer(ctx, o_slots + (size_t)P_ * cap * sizeof(mcg_particle), &wb);
+  if (rc != MCG_OK)
+    return rc;
+  unsigned long long *cnt = reinterpret_cast<unsigned long long *>(wb + o_c);
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(wb + o_rings, rings.data(), P_ * sizeof(mcg_aq_ring),
+                           cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess ||
+      (e = cudaMemsetAsync(cnt, 0, 64, ctx->stream)) != cudaSuccess)
+    return mcg_cuda_fail(e, "mcg_worker_run_async: set-up");
+  mcg_aq_init<<<ctx->sm_count * 4, 256, 0, ctx->stream>>>(
+      reinterpret_cast<unsigned long long *>(wb + o_seq), (unsigned long long)P_ * cap, cap);
+
+  const size_t smem_base = sizeof(mcg_libm_tab) + (size_t)((P_ + 1) & ~1) * sizeof(int2);
+  const bool use_smem = smem_base + (size_t)ctx->n_cells * 8 <= (size_t)ctx->smem_optin;
+  const size_t smem = smem_base + (use_smem ? (size_t)ctx->n_cells * 8 : 0);
+  if (smem > (size_t)ctx->smem_optin)
+    return mcg_fail(MCG_ERR_ARG, "mcg_worker_run_async: %d sub-domains too many", P_);
+  mcg_async_params A;
+  memset(&A, 0, sizeof(A));
+  A.cells = strict ? ctx->d_cells_strict : ctx->d_cells_fast;
+  A.n_layers = P_;
+  A.cell_lo = ctx->cell_lo;
+  A.n_cells = ctx->n_cells;
+  A.src_layer = src_layer;
+  A.rings = reinterpret_cast<mcg_aq_ring *>(wb + o_rings);
+  A.seq = reinterpret_cast<unsigned long long *>(wb + o_seq);
+  A.slots = reinterpret_cast<mcg_particle *>(wb + o_slots);
+  A.cap = cap;
+  A.src = *src;
+  A.src_next = cnt;
+  A.done = cnt + 1;
+  A.handoffs = cnt + 2;
+  A.src_total = (unsigned long long)n;
+  A.refill_steps = ctx->refill;
+  A.min_w = ctx->min_w;
+  A.q_log2 = ctx->log2_scale;
+  A.tally = ctx->d_tally;
+  A.counters = ctx->d_counters;
+  A.libm = ctx->libm;
+  A.libm_tab = ctx->libm_tab;
+  A.max_steps = ctx->max_steps;
+  A.idle_limit_ns = 2000000000ull; /* 2 s without any history finishing */
+  auto kern = strict ? (use_smem ? mcg_worker_async<true, true> : mcg_worker_async<true, false>)
+                     : (use_smem ? mcg_worker_async<false, true> : mcg_worker_async<false, false>);
+  int bps = 1;
+  if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                ctx->smem_optin)) != cudaSuccess ||
+      (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 1024, smem)) != cudaSuccess)
+    return mcg_cuda_fail(e, "mcg_worker_run_async: launch set-up");
+  cudaEventRecord(ctx->ev0, ctx->stream);
+  kern<<<ctx->sm_count * std::max(bps, 1), 1024, smem, ctx->stream>>>(A);
+  e = cudaGetLastError();
+  cudaEventRecord(ctx->ev1, ctx->stream);
+  if (e != cudaSuccess)
+    return mcg_cuda_fail(e, "mcg_worker_async launch");
+  ctx->launches++;
+  unsigned long long host[3] = {0, 0, 0};
+  if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess ||
+      (e = cudaMemcpy(host, cnt, sizeof(host), cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return mcg_cuda_fail(e, "mcg_worker_run_async");
+  cudaEventElapsedTime(&ctx->last_ms, ctx->ev0, ctx->ev1);
+  unsigned long long err = 0;
+  if ((e = cudaMemcpy(&err, ctx->d_counters + MCG_CNT_ERR, 8, cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return mcg_cuda_fail(e, "mcg_worker_run_async: error flags");
+  if (err & 2)
+    return mcg_fail(MCG_ERR_OVERFLOW, "mcg_worker_run_async: a hand-over ring overflowed "
+                    "(capacity %lld)", (long long)queue_capacity);
+  if (err & 4)
+    return mcg_fail(MCG_ERR_TIMEOUT, "mcg_worker_run_async: no history finished for %.1f s "
+                    "(%llu of %lld done)", A.idle_limit_ns * 1e-9, host[1], (long long)n);
+  if (err & 1)
+    return mcg_fail(MCG_ERR_LIMIT, "mcg_worker_run_async: a history exceeded the step limit");
+  unsigned long long hcount = (unsigned long long)n;
+  if ((e = cudaMemcpy(ctx->d_counters + MCG_CNT_HIST, &hcount, 8, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return mcg_cuda_fail(e, "mcg_worker_run_async: counters");
   if (h_handoffs)
     *h_handoffs = (int64_t)host[2];
   return MCG_OK;

@@ -28,3 +28,18 @@ def allreduce_tally(tally_q, group=None):
     assert tally_q.dtype == torch.int64
     dist.all_reduce(tally_q, op=dist.ReduceOp.SUM, group=group)
     return tally_q
+
+
+def sharded_tally(run_shard, n_total, world_size, rank, device=None, group=None):
+    """This rank's share of histories 0 .. n_total-1 run by
+    run_shard(first, count) -> int64 tally (numpy array or torch tensor), then
+    the exact sum over all ranks (allreduce_tally).  Returns the reduced int64
+    torch tensor on `device` (the GPU for NCCL, None for gloo on the CPU);
+    every rank holds the result, which equals one rank running every history."""
+    import numpy as np
+    import torch
+    first, count = shard(n_total, world_size, rank)
+    q = run_shard(first, count)
+    t = q if isinstance(q, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(q, np.int64))
+    t = t.to(device=device, dtype=torch.int64).contiguous()
+    return allreduce_tally(t, group=group)

@@ -4,14 +4,16 @@
  * sub-domain.
  *
  * The reference runs one Worker per MPI rank; here one Worker holds all
- * options.world_size sub-domains (the layers of decompose_domain) on the GPU
- * and spin() runs the workers' cycle with on-device hand-over queues
+ * options.world_size sub-domains (the layers of decompose_domain) on the GPU.
+ * WorkerSync::spin() runs the workers' cycle with on-device hand-over queues
  * (mcg_worker_run): each cycle every sub-domain simulates up to
  * nb_particles_per_cycle particles, leavers join the neighbour's queue, and
- * the loop ends when all nb_particles histories are finished.  The sync,
- * async and rma strategies of the reference differ only in how the MPI
- * messages travel; on one GPU they are the same queues, so WorkerSync,
- * WorkerAsync and WorkerRma name this class.  dump() writes out/config.yaml,
+ * the loop ends when all nb_particles histories are finished.
+ * WorkerAsync::spin() and WorkerRma::spin() run the asynchronous form
+ * (mcg_worker_run_async): one persistent launch, leavers handed to the
+ * neighbour's bounded ring and taken by whichever warp is idle, as
+ * AsyncComm/RmaComm let ranks proceed without a cycle barrier.  All three
+ * give the same tallies.  dump() writes out/config.yaml,
  * out/weights.csv, out/stats.csv and WA.out in the reference's formats
  * (src/worker.cpp:36-61, 63-181, 218-241, 287-313; src/layer.cpp:363-380).
  * stats.csv has WorkerSync's columns (the timer's, no message counts: the
@@ -51,8 +53,8 @@ class Worker
 {
 public:
   Worker(int world_rank, const MCMPIOptions &options);
-  ~Worker();
-  void spin();
+  virtual ~Worker();
+  virtual void spin();
   void dump();
   std::vector<real_t> weights_absorbed();
 
@@ -62,6 +64,9 @@ public:
   float seconds = 0.f;                /* GPU time of the last spin() */
   double starttime = 0.0, endtime = 0.0; /* wall clock (CLOCK_REALTIME) around spin() */
 
+protected:
+  bool async_ = false; /* spin() through mcg_worker_run_async */
+
 private:
   mcg_context *ctx_ = nullptr;
   std::vector<int32_t> start_, m_;
@@ -70,8 +75,29 @@ private:
   std::string foldername;
 };
 
-typedef Worker WorkerSync;
-typedef Worker WorkerAsync;
-typedef Worker WorkerRma;
+/* src/worker_sync.cpp: cycles with a hand-over barrier */
+class WorkerSync : public Worker
+{
+public:
+  using Worker::Worker;
+};
+
+/* src/worker_async.cpp: no cycle barrier (mcg_worker_run_async) */
+class WorkerAsync : public Worker
+{
+public:
+  WorkerAsync(int world_rank, const MCMPIOptions &options) : Worker(world_rank, options)
+  {
+    async_ = true;
+  }
+};
+
+/* src/worker_rma.cpp: one-sided puts into the neighbour's buffer are the same
+ * rings on one GPU */
+class WorkerRma : public WorkerAsync
+{
+public:
+  using WorkerAsync::WorkerAsync;
+};
 
 #endif

@@ -112,12 +112,19 @@ void Worker::spin()
   mcg_source src = {0, 1, 5127801, options.x_ini, 0.0f, (float)(1.0 / options.nb_particles),
                     (int32_t)(options.x_ini / dx_[src_layer])};
   int64_t cyc = 0, hand = 0;
-  const int64_t cap = (int64_t)options.nb_particles + 1;
   starttime = wall_seconds();
-  if (mcg_worker_run(ctx_, &src, (int64_t)options.nb_particles,
-                     options.nb_particles_per_cycle > 0 ? options.nb_particles_per_cycle : 65536,
-                     cap, &cyc, &hand) != MCG_OK)
-    die("Worker::spin");
+  if (async_) {
+    /* twice the resident threads of a GB300 (152 SMs x 1024) per ring */
+    if (mcg_worker_run_async(ctx_, &src, (int64_t)options.nb_particles, (int64_t)1 << 19,
+                             &hand) != MCG_OK)
+      die("WorkerAsync::spin");
+  } else {
+    const int64_t cap = (int64_t)options.nb_particles + 1;
+    if (mcg_worker_run(ctx_, &src, (int64_t)options.nb_particles,
+                       options.nb_particles_per_cycle > 0 ? options.nb_particles_per_cycle : 65536,
+                       cap, &cyc, &hand) != MCG_OK)
+      die("WorkerSync::spin");
+  }
   endtime = wall_seconds();
   cycles = cyc;
   handoffs = hand;

@@ -3,6 +3,7 @@
  * absorbed weight and the cycles; the files are checked by the caller. */
 #include <cstdio>
 #include <cstdlib>
+#include <vector>
 
 #include "worker.hpp"
 
@@ -20,5 +21,14 @@ int main(int argc, char **argv)
   for (real_t w : worker.weights_absorbed())
     total += w;
   printf("total %.9f cycles %lld handoffs %lld\n", total, worker.cycles, worker.handoffs);
+  /* the asynchronous workers on the same problem: the same weights */
+  WorkerAsync wa(0, opt);
+  wa.spin();
+  const std::vector<real_t> a = wa.weights_absorbed(), s = worker.weights_absorbed();
+  if (a != s) {
+    fprintf(stderr, "WorkerAsync and WorkerSync weights differ\n");
+    return EXIT_FAILURE;
+  }
+  printf("async handoffs %lld\n", wa.handoffs);
   return total > 0 ? 0 : EXIT_FAILURE;
 }

@@ -43,8 +43,12 @@ def test_reference_arm_other_ranks_exit_quietly():
 
 
 def test_conversion_roofline_arithmetic():
+    """64-bit conversions of the strict tracker: two per scatter (flight
+    sample and new direction), none per certain crossing; none in the fast
+    tracker; the peak is the smaller of the two measured 64-bit rates."""
     import bench
-    r = bench.conversion_roofline(10, 2, 1e-10, "strict")
-    assert r["achieved"] == 22 / 1e-10 and r["peak"] == bench.CONV64_PER_S
-    assert abs(r["frac"] - 22 / 1e-10 / bench.CONV64_PER_S) < 1e-12
-    assert bench.conversion_roofline(10, 2, 1.0, "fast")["achieved"] == 10
+    rates = {"u64_f32": 6e11, "f32_s64": 5.9e11, "u32_f32": 1e13, "f32_u32": 4.6e12}
+    r = bench.conversion_roofline(10, 2, 1e-10, "strict", rates)
+    assert r["achieved"] == 4 / 1e-10 and r["peak"] == 5.9e11
+    assert abs(r["frac"] - 4 / 1e-10 / 5.9e11) < 1e-12
+    assert bench.conversion_roofline(10, 2, 1.0, "fast", rates)["achieved"] == 0

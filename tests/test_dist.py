@@ -57,8 +57,22 @@ def _rank_main(rank, world, port, out_dir):
                              nthreads=1)
     t = torch.from_numpy(r["tally_q"].copy())
     dist.allreduce_tally(t)
+
+    # the code path of the benchmark's multi-rank check: dist.sharded_tally
+    # with each rank's share run by a callable (the GPU source there, the
+    # oracle standing in for it here)
+    def run_shard(f, c):
+        pp = np.zeros(c, O.PARTICLE_DTYPE)
+        pp["seed"] = O.rnd_seed_chain(O.lcg_skip(5127801, f, True), c)
+        pp["mu"], pp["wmc"] = 1.0, 1.0
+        return O.simulate_histories([O.layer_make(0.0, 1.0, 0, m)], sigs, rates, 1e-12, pp,
+                                    2.0 ** 40, nthreads=1)["tally_q"]
+
+    t2 = dist.sharded_tally(run_shard, n_total, world, rank)
+    np.save(os.path.join(out_dir, f"count{rank}.npy"), np.array([count]))
     if rank == 0:
         np.save(os.path.join(out_dir, "reduced.npy"), t.numpy())
+        np.save(os.path.join(out_dir, "sharded.npy"), t2.numpy())
     tdist.destroy_process_group()
 
 
@@ -79,3 +93,6 @@ def test_two_rank_gloo_reduction_is_exact(mcg, oracle, tmp_path):
     whole = oracle.simulate_histories([oracle.layer_make(0.0, 1.0, 0, m)], sigs, rates, 1e-12, p,
                                       2.0 ** 40)
     assert np.array_equal(reduced, whole["tally_q"])
+    assert np.array_equal(np.load(tmp_path / "sharded.npy"), whole["tally_q"])
+    # the two ranks ran different shards (1501 and 1500 histories)
+    assert [int(np.load(tmp_path / f"count{r}.npy")[0]) for r in (0, 1)] == [1501, 1500]

@@ -128,3 +128,71 @@ def test_libm_table_refused(built, mcg, tmp_path):
             del os.environ["MCG_LIBM_TABLE"]
         else:
             os.environ["MCG_LIBM_TABLE"] = old
+
+
+@pytest.mark.parametrize("fail_at", [0, 1, 2])
+def test_failed_layer_setup_leaves_no_geometry(built, mcg, fail_at):
+    """A device allocation that fails part-way through mcg_set_layers (made
+    to fail on the host, without touching the GPU) leaves the context with no
+    geometry: launches and tally reads return MCG_ERR_STATE instead of
+    indexing buffers sized for another chain; a new set-up recovers it and
+    gives the same tallies as a fresh context."""
+    lib = mcg.load_library()
+    p = np.zeros(64, mcg.PARTICLE_DTYPE)
+    p["seed"] = np.arange(1, 65, dtype=np.uint64) * np.uint64(104729)
+    p["mu"], p["wmc"] = 1.0, 1.0
+    with mcg.Context(mode="strict") as ref:
+        _slab(ref, 300)
+        ref.simulate(p.copy())
+        q_ref = ref.tally_q()
+    with mcg.Context(mode="strict") as ctx:
+        _slab(ctx, 200)
+        ctx.simulate(p.copy())
+        lib.mcg_testing_fail_allocation(fail_at)
+        try:
+            with pytest.raises(mcg.MCGError) as e:
+                _slab(ctx, 300)
+            assert e.value.code == 2  # MCG_ERR_CUDA
+        finally:
+            lib.mcg_testing_fail_allocation(-1)
+        rc, msg = _rc(mcg, "mcg_simulate", ctx.h, p.copy().ctypes.data_as(C.c_void_p), 64, None,
+                      None, None)
+        assert rc == 5 and "no layers" in msg
+        assert _rc(mcg, "mcg_tally_read", ctx.h, None, None)[0] == 5
+        _slab(ctx, 300)
+        ctx.simulate(p.copy())
+        assert np.array_equal(ctx.tally_q(), q_ref)
+
+
+@pytest.mark.parametrize("fail_at", [0, 3, 4])
+def test_failed_batch_setup_leaves_no_slabs(built, mcg, fail_at):
+    """The same for mcg_batch_set: a failed allocation leaves no slabs set
+    (MCG_ERR_STATE), and a new set-up runs as on a fresh context."""
+    lib = mcg.load_library()
+    rng = np.random.default_rng(11)
+    slabs = [dict(n_cells=int(c), n_histories=500, seed_mode=1, isotropic=s % 2,
+                  base_seed=1000 + 7919 * s, mu0=1.0, w0=1.0)
+             for s, c in enumerate(rng.integers(16, 200, 6))]
+    tot = sum(d["n_cells"] for d in slabs)
+    sigs = rng.uniform(0.5, 5.0, tot).astype(np.float32)
+    rates = rng.uniform(0.1, 0.9, tot).astype(np.float32)
+    with mcg.Context(mode="strict") as ref:
+        ref.batch_set(slabs, sigs, rates, 1e-12)
+        ref.batch_run()
+        q_ref = ref.batch_tally_q()
+    with mcg.Context(mode="strict") as ctx:
+        ctx.batch_set(slabs[:3], sigs[: sum(d["n_cells"] for d in slabs[:3])],
+                      rates[: sum(d["n_cells"] for d in slabs[:3])], 1e-12)
+        ctx.batch_run()
+        lib.mcg_testing_fail_allocation(fail_at)
+        try:
+            with pytest.raises(mcg.MCGError) as e:
+                ctx.batch_set(slabs, sigs, rates, 1e-12)
+            assert e.value.code == 2
+        finally:
+            lib.mcg_testing_fail_allocation(-1)
+        rc, msg = _rc(mcg, "mcg_batch_run", ctx.h)
+        assert rc == 5 and "no slabs" in msg
+        ctx.batch_set(slabs, sigs, rates, 1e-12)
+        ctx.batch_run()
+        assert np.array_equal(ctx.batch_tally_q(), q_ref)

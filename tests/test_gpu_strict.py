@@ -363,6 +363,37 @@ def test_worker_handover_queues_match_fused(mcg, per_cycle):
         assert cycles > 10 and hand > 4000
 
 
+@pytest.mark.parametrize("mode", ["strict", "fast"])
+def test_async_worker_matches_fused(mcg, mode):
+    """The asynchronous workers (one persistent launch, bounded rings per
+    sub-domain) give the fused tracker's tallies and step counts exactly, on
+    repeated calls that reuse the context's rings; a smaller capacity than
+    the hand-over traffic needs is reported as MCG_ERR_OVERFLOW and the
+    context stays usable."""
+    st, m, dx, sigs, rates = _slab(mcg, 10000, 64)
+    with mcg.Context(mode=mode) as ctx:
+        ctx.set_layers(st, m, dx, sigs, rates, 1e-12)
+        ctx.simulate_source(0, 20000)
+        fused = ctx.tally_q()
+        c_fused = ctx.counters()
+        for _ in range(2):
+            ctx.tally_reset()
+            hand = ctx.worker_run_async(20000)
+            assert np.array_equal(ctx.tally_q(), fused)
+            c = ctx.counters()
+            assert c["steps"] == c_fused["steps"] and c["scatters"] == c_fused["scatters"]
+            assert c["histories"] == 20000 and hand > 20000
+        ctx.tally_reset()
+        with pytest.raises(mcg.MCGError) as e:
+            ctx.worker_run_async(200000, queue_capacity=4)
+        assert e.value.code == 3  # MCG_ERR_OVERFLOW
+        ctx.tally_reset()
+        ctx.worker_run_async(0)
+        assert ctx.tally_q().sum() == 0
+        ctx.worker_run_async(20000)
+        assert np.array_equal(ctx.tally_q(), fused)
+
+
 def test_worker_matches_reference_workersync_tally(mcg):
     """Against the reference's own Layer::simulate driven by the WorkerSync
     cycle (golden fixture): float tallies agree to float accuracy."""
