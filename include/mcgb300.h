@@ -390,9 +390,10 @@ int mcg_rnd_real_device(mcg_context *ctx, uint64_t *d_seeds, float *d_reals, int
  * [0, 1], fn 1 expf on [-17.5, 89) (other arguments give NaN); fn 2 the
  * hardware 2^x of the strict tracker's certain-crossing test; fn 3 expf
  * like fn 1 but through the evaluator's general path for every argument;
- * fn 4 the hardware log2, fn 5 the flight log2 of a float sample h,
- * fn 6 the fast arithmetic's flight log2 of the sample whose state has top
- * 32 bits t, t passed as the argument's bit pattern. */
+ * fn 4 the hardware log2, fn 5 the fast arithmetic's collision probability
+ * 1 - e^-tau of a flight of optical depth tau >= 0, fn 6 the fast
+ * arithmetic's log2 of the flight sample whose state has top 32 bits t
+ * (t passed as the argument's bit pattern). */
 int mcg_libm_eval_device(mcg_context *ctx, int fn, const float *d_in, float *d_out, int64_t n);
 
 /* Check of the strict tracker's division by a cached reciprocal against the

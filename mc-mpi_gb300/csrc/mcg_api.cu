@@ -323,7 +323,7 @@ void mcg_cell_params(float sig, float rate, int gi, float dx, float4 &strict, fl
   const float sig_i = sig * interaction_rate;
   const float elo = (float)gi * dx, ehi = (float)(gi + 1) * dx;
   strict = make_float4(sig_a, sig_i, elo, ehi);
-  fast = make_float4(sig_a, sig_i > 1e-4f ? (float)(-0.69314718055994530942 / (double)sig_i) : 0.0f,
+  fast = make_float4(sig_a, sig_i > 1e-4f ? sig_i : 0.0f,
                      elo, ehi);
 }
 
@@ -435,7 +435,7 @@ extern "C" int mcg_set_layers_xs(mcg_context *ctx, int n_layers, const int32_t *
       float4 &cs = ctx->cells_strict[k], &cf = ctx->cells_fast[k];
       cs.x = cf.x = h_sig_a[k];
       cs.y = h_sig_s[k];
-      cf.y = h_sig_s[k] > 1e-4f ? (float)(-0.69314718055994530942 / (double)h_sig_s[k]) : 0.0f;
+      cf.y = h_sig_s[k] > 1e-4f ? h_sig_s[k] : 0.0f;
     }
   update_thin(ctx);
   cudaError_t e;

@@ -82,7 +82,7 @@ __device__ __forceinline__ float mcg_rnd_real(uint64_t &s)
  * (two integer/float operations instead of an exact 64-bit rounding).  The
  * subtraction from [1, 2) of 1 - 2^-24 is exact (Sterbenz).  The midpoint
  * makes mu = 2h - 1 symmetric about 0 and h never 0.  (Flight samples use
- * mcg_flight_log2, at 2^-32 resolution.) */
+ * mcg_flight_u, at 2^-32 resolution.) */
 __device__ __forceinline__ float mcg_rnd_real_fast(uint64_t &s)
 {
   mcg_lcg_next(s);
@@ -281,18 +281,25 @@ __device__ __forceinline__ float mcg_expf_strict(float t, const mcg_libm_tab *T,
   return y;
 }
 
-/* log2(h) of the fast arithmetic's flight sample, drawn from the state s
- * (already advanced) at 2^-32 resolution: t = the state's top 32 bits,
- * h = (t + 1/2) 2^-32, u = 1 - h = (~t + 1/2) 2^-32.  A thin cell's collision
- * probability per crossing is ~1e-4 (10,000-cell slab), decided by u within
- * ~1e-4 of 0, so u must be fine-grained there: on a 2^-23 grid it shifts each
- * cell's collision probability by up to half a grid step (3e-4 relative rms
- * per cell against the reference's 2^-24 grid), a 2^-32 grid by ~1e-6.
- * Near 1 (u < 2^-8, u exact below 2^-9 and within 2^-24 relative above) the
- * series -ln(1 - u) = u (1 + u/2 + u^2/3) (truncation below 2^-26
- * relative); elsewhere the hardware log2 of h = RN(1 - u), documented to an
- * absolute error of 2^-22 on [0.5, 2], which near 1 would be a relative error
- * of a few 1e-4 in the flight test. */
+/* The fast arithmetic's flight sample, drawn from the state s (already
+ * advanced) at 2^-32 resolution: t = the state's top 32 bits,
+ * h = (t + 1/2) 2^-32 and u = 1 - h = (~t + 1/2) 2^-32 (exact for u < 2^-9,
+ * within 2^-24 relative above).  A thin cell's collision probability per
+ * crossing is ~1e-4 (10,000-cell slab), decided by u within ~1e-4 of 0, so
+ * u must be fine-grained there: on a 2^-23 grid it shifts each cell's
+ * collision probability by up to half a grid step (3e-4 relative rms per
+ * cell against the reference's 2^-24 grid), a 2^-32 grid by ~1e-6. */
+__device__ __forceinline__ float mcg_flight_u(uint64_t s)
+{
+  return __fmaf_rn(__uint2float_rn(~(uint32_t)(s >> 31)), 0x1p-32f, 0x1p-33f);
+}
+
+/* log2(h) of that sample, for the distance of a collision: near 1
+ * (u < 2^-8) the series -ln(1 - u) = u (1 + u/2 + u^2/3) (truncation below
+ * 2^-26 relative); elsewhere the hardware log2 of h computed from t
+ * directly (so h keeps its relative precision when it is small), documented
+ * to an absolute error of 2^-22 on [0.5, 2], which near 1 would be a
+ * relative error of a few 1e-4. */
 __device__ __forceinline__ float mcg_flight_log2(uint64_t s)
 {
   const uint32_t t = (uint32_t)(s >> 31);
@@ -300,19 +307,17 @@ __device__ __forceinline__ float mcg_flight_log2(uint64_t s)
   float p = fmaf(u, MCG_LOG2E_F * (1.0f / 3.0f), MCG_LOG2E_F * 0.5f);
   p = fmaf(u, p, MCG_LOG2E_F);
   const float near1 = -u * p;
-  return u < 0x1p-8f ? near1 : __log2f(__fsub_rn(1.0f, u));
+  return u < 0x1p-8f ? near1 : __log2f(__fmaf_rn(__uint2float_rn(t), 0x1p-32f, 0x1p-33f));
 }
 
-/* The former flight log2 on a float sample h in (0, 1) (the midpoint grid
- * of mcg_rnd_real_fast): the series for u = 1 - h < 2^-8, else the hardware
- * log2.  Kept as a testing aid (mcg_libm_eval_device fn 5). */
-__device__ __forceinline__ float mcg_log2_flight(float h)
+/* 1 - e^t for |t| < 2^-7: -t (1 + t/2 + t^2/6 + t^3/24), truncation below
+ * 2^-31 relative. */
+__device__ __forceinline__ float mcg_one_minus_exp_small(float t)
 {
-  const float u = __fsub_rn(1.0f, h);
-  float p = fmaf(u, MCG_LOG2E_F * (1.0f / 3.0f), MCG_LOG2E_F * 0.5f);
-  p = fmaf(u, p, MCG_LOG2E_F);
-  const float near1 = -u * p;
-  return u < 0x1p-8f ? near1 : __log2f(h);
+  float p = fmaf(t, 1.0f / 24.0f, 1.0f / 6.0f);
+  p = fmaf(t, p, 0.5f);
+  p = fmaf(t, p, 1.0f);
+  return -t * p;
 }
 
 /* Fast build: 1 - e^t for t <= 0 to a few ulp without cancellation. */

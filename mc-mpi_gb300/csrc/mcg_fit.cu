@@ -353,7 +353,7 @@ extern "C" int mcg_fit_set(mcg_context *ctx, int32_t n_slabs, const mcg_slab *h_
     sd[s].src = {sl.seed_mode, sl.isotropic, sl.base_seed, 0.0f, sl.mu0, sl.w0, 0};
     for (int j = 0; j < sl.n_cells; ++j, ++k) {
       const float sig_s = h_sig_s[k];
-      cf[k] = make_float4(h_sig_a0[k], sig_s > 1e-4f ? (float)(-0.69314718055994530942 / (double)sig_s) : 0.0f,
+      cf[k] = make_float4(h_sig_a0[k], sig_s > 1e-4f ? sig_s : 0.0f,
                           (float)j * dx, (float)(j + 1) * dx);
       cs[k] = s;
     }

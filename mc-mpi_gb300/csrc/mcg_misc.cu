@@ -33,8 +33,11 @@ __global__ void mcg_libm_eval_kernel(int fn, const float *in, float *out, int64_
       r = mcg_ex2_approx(v);
     else if (fn == 4)
       r = __log2f(v);
-    else if (fn == 5)
-      r = mcg_log2_flight(v);
+    else if (fn == 5) {
+      /* the fast step's collision probability 1 - e^-tau of optical depth
+       * tau >= 0, as mcg_fast_flight computes it */
+      r = fabsf(v) < 0x1p-7f ? mcg_one_minus_exp_small(-v) : mcg_one_minus_exp_fast(-v);
+    }
     else if (fn == 6)
       /* the fast flight sample's log2 from the state's top 32 bits t,
        * passed as the argument's bit pattern */

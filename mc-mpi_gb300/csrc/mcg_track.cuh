@@ -21,7 +21,7 @@
 #include "mcgb300.h"
 
 /* Per-cell step parameters.  strict: {sig_a, sig_i, edge_lo, edge_hi}
- * fast: {sig_a, -ln2/sig_i (0 when sig_i <= EPS), edge_lo, edge_hi}
+ * fast: {sig_a, sig_i (0 when sig_i <= EPS), edge_lo, edge_hi}
  * edge_lo = (float)i * dx_layer, edge_hi = (float)(i+1) * dx_layer with the
  * GLOBAL cell index i and the cell's own layer spacing (src/layer.cpp:146,150). */
 struct mcg_track_params {
@@ -138,8 +138,35 @@ __device__ __forceinline__ void mcg_load_particle(const mcg_track_params &P, int
   }
 }
 
+/* The fast step's flight: the crossing's absorption 1 - e^(-sig_a de) into
+ * om_cross, and whether the flight ends in a collision before the face, the
+ * event -ln(1 - u) / sig_i < de of the reference's test evaluated as
+ * u < 1 - e^(-sig_i de) (no logarithm per step; the collision's distance is
+ * computed only when it happens).  sig_i = 0 when it is at most EPS (never a
+ * collision, as the reference's di = MAXREAL). */
+__device__ __forceinline__ bool mcg_fast_flight(uint64_t seed, float sig_a, float sig_i, float de,
+                                                float &om_cross)
+{
+  const float ta = -sig_a * de, ti = -sig_i * de;
+  float p;
+  if (fmaxf(fabsf(ta), fabsf(ti)) < 0x1p-7f) {
+    om_cross = mcg_one_minus_exp_small(ta);
+    p = mcg_one_minus_exp_small(ti);
+  } else {
+    om_cross = mcg_one_minus_exp_fast(ta);
+    p = mcg_one_minus_exp_fast(ti);
+  }
+  return mcg_flight_u(seed) < p;
+}
+
+/* Distance of the fast step's collision: -ln(1 - u) / sig_i, at most de. */
+__device__ __forceinline__ float mcg_fast_collision_distance(uint64_t seed, float sig_i, float de)
+{
+  return fminf(mcg_flight_log2(seed) * __fdividef(-0.6931472f, sig_i), de);
+}
+
 /* One Layer::particle_step (src/layer.cpp:123-190) on a lane's particle in
- * cell c = {sig_a, sig_i or -ln2/sig_i, edge_lo, edge_hi}; deposits into
+ * cell c = {sig_a, sig_i (fast: 0 when at most EPS), edge_lo, edge_hi}; deposits into
  * *tally_cell.  STRICT: the reference's float operations and host-libm
  * logf/expf; the crossing's absorption is computed before the logarithm and
  * a certified exponential bound settles most crossings without it (see
@@ -238,11 +265,11 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
     }
   } else {
     const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
-    const float om_cross = mcg_one_minus_exp_fast(-sig_a * de);
-    const float di = c.y != 0.0f ? mcg_flight_log2(seed) * c.y : MCG_MAXREAL;
-    const bool coll = di < de;
+    float om_cross;
+    const bool coll = mcg_fast_flight(seed, sig_a, c.y, de, om_cross);
+    const float di = coll ? mcg_fast_collision_distance(seed, c.y, de) : de;
     if (l_out) {
-      *l_out = coll ? di : de;
+      *l_out = di;
       *coll_out = coll;
     }
     if (coll) {
@@ -271,7 +298,7 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
 }
 
 /* One Layer::particle_step (src/layer.cpp:123-190) on a lane's particle in
- * cell c = {sig_a, sig_i or -ln2/sig_i, edge_lo, edge_hi}, in two parts, for
+ * cell c = {sig_a, sig_i (fast: 0 when at most EPS), edge_lo, edge_hi}, in two parts, for
  * the event-based tracker: mcg_step_cross advances the state to the flight
  * sample's and completes the step when it is a certain crossing (STRICT: the
  * branch-free path of mcg_step; FAST: the flight ends past the edge),
@@ -327,14 +354,13 @@ __device__ __forceinline__ bool mcg_step_cross(uint64_t &seed, float &x, float &
     }
   } else {
     const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
-    const float di = c.y != 0.0f ? mcg_flight_log2(seed) * c.y : MCG_MAXREAL;
-    if (di < de)
+    float om;
+    if (mcg_fast_flight(seed, sig_a, c.y, de, om))
       return false;
     if (l_out) {
       *l_out = de;
       *coll_out = false;
     }
-    const float om = mcg_one_minus_exp_fast(-sig_a * de);
     x = edge;
     /* deposit the weight actually removed (exact by Sterbenz while the new
      * weight is at least half the old), so the tally plus the surviving
@@ -407,11 +433,11 @@ __device__ __forceinline__ void mcg_step_rest(uint64_t &seed, float &x, float &m
     }
   } else {
     const float de = inv_mu != 0.0f ? (edge - x) * inv_mu : MCG_MAXREAL;
-    const float om_cross = mcg_one_minus_exp_fast(-sig_a * de);
-    const float di = c.y != 0.0f ? mcg_flight_log2(seed) * c.y : MCG_MAXREAL;
-    const bool coll = di < de;
+    float om_cross;
+    const bool coll = mcg_fast_flight(seed, sig_a, c.y, de, om_cross);
+    const float di = coll ? mcg_fast_collision_distance(seed, c.y, de) : de;
     if (l_out) {
-      *l_out = coll ? di : de;
+      *l_out = di;
       *coll_out = coll;
     }
     if (coll) {

@@ -95,13 +95,40 @@ def test_flight_log2_accurate_near_one(built, mcg):
     assert np.abs(rel[near]).max() <= 2.0 ** -21
     assert abs(rel[near].mean()) <= 1e-7
     assert np.abs(rel[~near]).max() <= 2.0 ** -14
-    # the collision probability of a flight of optical depth tau is the share
-    # of t whose sample gives -ln h < tau: within 2^-32 of 1 - e^-tau
-    # (every t with u < 2^-8 is in the first half of the array)
-    for tau in (1e-6, 3e-4, 3e-3):
-        p_exact = -np.expm1(-tau)
-        k = np.count_nonzero(-got[: 1 << 24] * np.log(2.0) < tau)
-        assert abs(k * 2.0 ** -32 - p_exact) <= 2 * 2.0 ** -32 + 2.0 ** -21 * p_exact
+
+
+def test_fast_collision_probability(built, mcg):
+    """The fast step decides a collision by u < p(tau), p = 1 - e^-tau (fn 5)
+    for the flight's optical depth tau to the face, u = (~t + 1/2) 2^-32 from
+    the state's top 32 bits t: p within 2^-21 relative of -expm1(-tau) for
+    tau < 2^-7 (the series) and 2^-19 above (1 - the hardware exp), and the
+    share of the 2^32 values of t that collide within 2^-32 of p, so the
+    collision probability of every flight is unbiased to ~1e-6 relative even
+    in a 10,000-cell slab's thin cells (p ~ 1e-4)."""
+    import torch
+    tau = np.concatenate([np.geomspace(1e-9, 2.0 ** -7, 200000, endpoint=False),
+                          np.geomspace(2.0 ** -7, 60.0, 200000)]).astype(np.float32)
+    exact = -np.expm1(-tau.astype(np.float64))
+    with mcg.Context(mode="strict") as ctx:
+        ctx.set_layers([0], [1], [np.float32(1.0)], np.ones(1, np.float32),
+                       np.full(1, 0.5, np.float32), 1e-12)
+        ctx.simulate_source(0, 4)
+        d_in = torch.from_numpy(tau).cuda()
+        d_out = torch.empty_like(d_in)
+        torch.cuda.synchronize()
+        ctx.libm_eval_device(5, d_in.data_ptr(), d_out.data_ptr(), len(tau))
+        p = d_out.cpu().numpy().astype(np.float64)
+    rel = np.abs(p - exact) / exact
+    small = tau < 2.0 ** -7
+    assert rel[small].max() <= 2.0 ** -21 and rel[~small].max() <= 2.0 ** -19
+    # the share of t with u_t < p: u_t increases as t decreases, so the count
+    # is the number of k = ~t with (k + 1/2) 2^-32 (rounded as the device) < p
+    k = np.arange(1 << 24, dtype=np.uint64)
+    u = k.astype(np.float32) * np.float32(2.0 ** -32) + np.float32(2.0 ** -33)
+    for j in (0, 50000, 150000, 190000):
+        n = int(np.count_nonzero(u < np.float32(p[j])))
+        assert n < (1 << 24)
+        assert abs(n * 2.0 ** -32 - exact[j]) <= 2 * 2.0 ** -32 + 2.0 ** -21 * exact[j]
 
 
 def _fp64_fixture(size):
