@@ -266,6 +266,8 @@ void mcg_ext_destroy(mcg_context *ctx)
   mcg_adjoint_release(&ctx->ext->adj);
   if (ctx->ext->worker.dev)
     cudaFree(ctx->ext->worker.dev);
+  if (ctx->ext->worker.monitor)
+    cudaStreamDestroy(ctx->ext->worker.monitor);
   delete ctx->ext;
   ctx->ext = nullptr;
 }

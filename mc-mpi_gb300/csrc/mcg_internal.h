@@ -57,6 +57,7 @@ struct mcg_fit_state; /* mcg_fit.cu */
 struct mcg_worker_state {
   void *dev = nullptr;
   size_t bytes = 0;
+  cudaStream_t monitor = nullptr; /* progress reads and the abort word */
 };
 
 struct mcg_ext {

@@ -23,6 +23,10 @@
  * Per-particle trajectories, hence tallies, equal the fused tracker's.
  */
 #include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <thread>
 #include <cstring>
 #include <vector>
 
@@ -436,7 +440,7 @@ extern "C" int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n
 /* ---------------------------------------------------------------------------
  * The asynchronous form (WorkerAsync / WorkerRma, src/worker_async.cpp:19-105,
  * src/async_comm.cpp, src/rma_comm.cpp): no cycles.  One persistent launch;
- * every warp takes work for its idle lanes from any sub-domain's queue (or
+ * every warp takes work for its idle lanes from the sub-domains' queues (or
  * newborns from the source), simulates each particle inside its sub-domain
  * and appends leavers to the neighbour's queue, until the device counter of
  * finished histories reaches N.  The queues are bounded multi-producer
@@ -448,10 +452,20 @@ extern "C" int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n
  * reading, frees the slots for the next lap (seq = t + C).  Nothing waits on
  * a slot: a producer that finds its slot still occupied (the ring holds C
  * particles) sets the overflow flag, as the reference aborts on a full
- * buffer.  Warps without work sleep briefly and poll; they give up with
- * MCG_ERR_TIMEOUT after `idle_limit_ns` without any history finishing.
- * Every particle follows the trajectory of the fused tracker, so the tally
- * equals it.
+ * buffer.
+ *
+ * Idle warps must not crowd the rings: a global count of published,
+ * unclaimed particles (a hint, exact once every producer and consumer has
+ * updated it) is all an idle warp polls, with an exponential back-off sleep
+ * (up to 32 us); only when it is positive does the warp look at the rings,
+ * each lane one or two rings at once, and try to claim from at most four.
+ * The grid is no larger than the work needs (one 1024-thread block per 1024
+ * histories).  Every loop of the kernel is bounded: a warp gives up with
+ * MCG_ERR_TIMEOUT after `idle_limit_ns` in which no history finished, and
+ * every warp, busy or not, stops at the launch's deadline (`budget_ns` after
+ * its start), recording how far the run got, so a run can fail but never
+ * hang.  Every particle follows the trajectory of the fused tracker, so the
+ * tally equals it.
  * ------------------------------------------------------------------------- */
 struct mcg_aq_ring {
   int32_t lo, hi;           /* cell range of the sub-domain (global indices) */
@@ -459,6 +473,10 @@ struct mcg_aq_ring {
   unsigned long long deq;   /* tickets claimed by consumers */
   unsigned long long pad[5];
 };
+
+/* Run state of the asynchronous workers (one 256-byte block of counters). */
+enum { MCG_AQ_SRC_NEXT = 0, MCG_AQ_DONE, MCG_AQ_HANDOFFS, MCG_AQ_PENDING, MCG_AQ_DEADLINE_HITS,
+       MCG_AQ_ABORT, MCG_AQ_ITERS, MCG_AQ_EXITED, MCG_AQ_N };
 
 struct mcg_async_params {
   const float4 *cells;
@@ -468,22 +486,29 @@ struct mcg_async_params {
   unsigned long long *seq;      /* n_layers x cap publication words */
   unsigned long long cap;
   mcg_source src;
-  unsigned long long *src_next; /* newborns handed out so far */
+  unsigned long long *state;    /* MCG_AQ_* counters */
   unsigned long long src_total;
   int32_t refill_steps;
   float min_w;
   int32_t q_log2;
-  unsigned long long *tally, *counters, *done, *handoffs;
+  unsigned long long *tally, *counters;
   mcg_libm_dev libm;
   const mcg_libm_tab *libm_tab;
   uint32_t max_steps;
-  unsigned long long idle_limit_ns;
+  unsigned long long idle_limit_ns, budget_ns;
 };
 
 __device__ __forceinline__ unsigned long long mcg_ld_acquire(const unsigned long long *p)
 {
   unsigned long long v;
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long mcg_ld_relaxed(const unsigned long long *p)
+{
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
 
@@ -522,82 +547,108 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
   const float min_w = P.min_w;
   const int qs = P.q_log2;
   const unsigned long long cap = P.cap;
+  const int nl = P.n_layers;
+  unsigned long long *const src_next = P.state + MCG_AQ_SRC_NEXT;
+  unsigned long long *const done = P.state + MCG_AQ_DONE;
+  long long *const pending = reinterpret_cast<long long *>(P.state + MCG_AQ_PENDING);
 
   uint64_t seed = 0;
   float x = 0.f, mu = 0.f, wmc = 0.f, inv_mu = 0.f;
   int idx = 0, L = 0, llo = 0, lhi = 0;
   uint32_t nst = 0, nsc = 0;
   bool active = false;
-  unsigned long long n_done = 0, n_hand = 0, steps = 0, scat = 0;
+  unsigned long long n_hand = 0, steps = 0, scat = 0;
   unsigned long long seen_done = 0, seen_t = 0;
-  int scan = gwarp % P.n_layers;
-  bool timed_out = false;
+  /* every decision that steers the warp's control flow is taken on lane
+   * 0's value, broadcast, so the lanes can never disagree */
+  const unsigned long long t_start = __shfl_sync(0xffffffffu, mcg_globaltimer(), 0);
+  unsigned long long iters = 0;
+  int scan = gwarp % nl;
+  unsigned sleep_ns = 128;
+  unsigned long long stop = 0; /* 4: idle limit, 8: deadline */
 
   for (;;) {
     unsigned need = __ballot_sync(0xffffffffu, !active);
     if (need) {
-      /* 1. queued particles: scan the rings from this warp's rotating start
-       * and claim a run of published tickets of the first ring that has some */
-      for (int probe = 0; probe < P.n_layers && need; ++probe) {
-        const int l = (scan + probe) % P.n_layers;
-        mcg_aq_ring *R = &P.rings[l];
-        unsigned long long h = 0, e = 0;
-        if (lane == 0) {
-          h = *(volatile unsigned long long *)&R->deq;
-          e = *(volatile unsigned long long *)&R->enq;
+      /* 1. queued particles, when the published count says there are some:
+       * each lane looks at one or two rings from this warp's rotating
+       * start; the warp tries to claim a run of published tickets from at
+       * most four of the non-empty ones */
+      long long pend = 0;
+      if (lane == 0)
+        pend = (long long)mcg_ld_relaxed(reinterpret_cast<unsigned long long *>(pending));
+      pend = __shfl_sync(0xffffffffu, pend, 0);
+      if (pend > 0) {
+        const int r0 = (scan + lane) % nl, r1 = (scan + lane + 32) % nl;
+        const bool ne0 = lane < nl && mcg_ld_relaxed(&P.rings[r0].enq) > mcg_ld_relaxed(&P.rings[r0].deq);
+        const bool ne1 = lane + 32 < nl && mcg_ld_relaxed(&P.rings[r1].enq) > mcg_ld_relaxed(&P.rings[r1].deq);
+        unsigned long long cand = ((unsigned long long)__ballot_sync(0xffffffffu, ne1) << 32) |
+                                  __ballot_sync(0xffffffffu, ne0);
+        for (int tries = 0; tries < 4 && cand && need; ++tries) {
+          const int j = __ffsll((long long)cand) - 1;
+          cand &= cand - 1;
+          const int l = (scan + j) % nl;
+          mcg_aq_ring *R = &P.rings[l];
+          unsigned long long h = 0, e = 0;
+          if (lane == 0) {
+            h = mcg_ld_relaxed(&R->deq);
+            e = mcg_ld_relaxed(&R->enq);
+          }
+          h = __shfl_sync(0xffffffffu, h, 0);
+          e = __shfl_sync(0xffffffffu, e, 0);
+          if (e <= h)
+            continue;
+          const unsigned long long want = min((unsigned long long)__popc(need), e - h);
+          const bool pub = (unsigned long long)lane < want &&
+                           mcg_ld_relaxed(&P.seq[(size_t)l * cap + (h + lane) % cap]) == h + lane + 1;
+          const unsigned pubmask = __ballot_sync(0xffffffffu, pub);
+          const int m = pubmask == 0xffffffffu ? 32 : __ffs(~pubmask) - 1; /* leading run */
+          if (m <= 0)
+            continue;
+          unsigned long long got = 0;
+          if (lane == 0)
+            got = atomicCAS(&R->deq, h, h + (unsigned long long)m);
+          got = __shfl_sync(0xffffffffu, got, 0);
+          if (got != h)
+            continue; /* another warp claimed first */
+          if (lane == 0)
+            atomicAdd(reinterpret_cast<unsigned long long *>(pending), (unsigned long long)(-(long long)m));
+          const int rank = __popc(need & lanemask_lt());
+          if (((need >> lane) & 1u) && rank < m) {
+            const unsigned long long t = h + rank;
+            const size_t s = (size_t)l * cap + t % cap;
+            /* the reading lane acquires the publication itself (another lane
+             * saw it published, so this returns at once; bounded anyway) */
+            int polls = 0;
+            while (mcg_ld_acquire(&P.seq[s]) != t + 1 && ++polls < (1 << 16))
+              __nanosleep(64);
+            if (polls >= (1 << 16))
+              atomicOr(&P.counters[MCG_CNT_ERR], 16ull);
+            const mcg_particle q = P.slots[s];
+            mcg_st_release(&P.seq[s], t + cap); /* free for the next lap */
+            seed = q.seed, x = q.x, mu = q.mu, wmc = q.wmc, idx = q.index - P.cell_lo;
+            L = l;
+            llo = s_rng[l].x;
+            lhi = s_rng[l].y;
+            inv_mu = mcg_flight_rcp(mu);
+            nst = nsc = 0;
+            active = true;
+          }
+          need = __ballot_sync(0xffffffffu, !active);
         }
-        h = __shfl_sync(0xffffffffu, h, 0);
-        e = __shfl_sync(0xffffffffu, e, 0);
-        if (e <= h)
-          continue;
-        const int cnt = __popc(need);
-        const unsigned long long want = min((unsigned long long)cnt, e - h);
-        const bool pub = (unsigned long long)lane < want &&
-                         mcg_ld_acquire(&P.seq[(size_t)l * cap + (h + lane) % cap]) == h + lane + 1;
-        const unsigned pubmask = __ballot_sync(0xffffffffu, pub);
-        /* leading published tickets */
-        const int m = pubmask == 0xffffffffu ? 32 : __ffs(~pubmask) - 1;
-        if (m <= 0)
-          continue;
-        unsigned long long got = 0;
-        if (lane == 0)
-          got = atomicCAS(&R->deq, h, h + (unsigned long long)m);
-        got = __shfl_sync(0xffffffffu, got, 0);
-        if (got != h)
-          continue; /* another warp claimed first: look again later */
-        __syncwarp();
-        const int rank = __popc(need & lanemask_lt());
-        if ((need >> lane) & 1u && rank < m) {
-          const unsigned long long t = h + rank;
-          const size_t s = (size_t)l * cap + t % cap;
-          /* the reading lane acquires the publication itself (another lane
-           * of the warp saw it, so this returns at once) */
-          int tries = 0;
-          while (mcg_ld_acquire(&P.seq[s]) != t + 1 && ++tries < (1 << 20))
-            ;
-          if (tries >= (1 << 20))
-            atomicOr(&P.counters[MCG_CNT_ERR], 4ull);
-          const mcg_particle q = P.slots[s];
-          mcg_st_release(&P.seq[s], t + cap); /* free for the next lap */
-          seed = q.seed, x = q.x, mu = q.mu, wmc = q.wmc, idx = q.index - P.cell_lo;
-          L = l;
-          llo = s_rng[l].x;
-          lhi = s_rng[l].y;
-          inv_mu = mcg_flight_rcp(mu);
-          nst = nsc = 0;
-          active = true;
-        }
-        need = __ballot_sync(0xffffffffu, !active);
       }
       /* 2. newborns from the source for the lanes still idle */
-      if (need && *(volatile unsigned long long *)P.src_next < P.src_total) {
-        const int cnt = __popc(need);
+      unsigned long long sn = 0;
+      if (lane == 0)
+        sn = mcg_ld_relaxed(src_next);
+      sn = __shfl_sync(0xffffffffu, sn, 0);
+      if (need && sn < P.src_total) {
         unsigned long long base = 0;
         if (lane == 0)
-          base = atomicAdd(P.src_next, (unsigned long long)cnt);
+          base = atomicAdd(src_next, (unsigned long long)__popc(need));
         base = __shfl_sync(0xffffffffu, base, 0);
         const int rank = __popc(need & lanemask_lt());
-        if ((need >> lane) & 1u && base + rank < P.src_total) {
+        if (((need >> lane) & 1u) && base + rank < P.src_total) {
           mcg_source_particle(P.src, (int64_t)(base + rank), seed, x, mu, wmc, idx);
           idx -= P.cell_lo;
           L = P.src_layer;
@@ -608,29 +659,46 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
           active = true;
         }
       }
-      scan = (scan + 1) % P.n_layers;
+      scan = (scan + 1) % nl;
     }
+    ++iters;
+    unsigned long long now = 0, errw = 0;
+    if (lane == 0) {
+      now = mcg_globaltimer();
+      errw = mcg_ld_relaxed(&P.counters[MCG_CNT_ERR]) | mcg_ld_relaxed(&P.state[MCG_AQ_ABORT]);
+    }
+    now = __shfl_sync(0xffffffffu, now, 0);
+    errw = __shfl_sync(0xffffffffu, errw, 0);
+    if (now - t_start > P.budget_ns || (errw & 32ull)) {
+      /* the launch's deadline, or the host's abort: abandon what this warp
+       * holds */
+      stop = 8;
+      break;
+    }
+    if (errw & 30ull)
+      break; /* a full ring, or another warp gave up */
     if (!__any_sync(0xffffffffu, active)) {
-      /* nothing to do: finished, or wait for other warps' hand-overs */
+      /* nothing to do: finished, or wait (backing off) for hand-overs */
       unsigned long long d = 0;
       if (lane == 0)
-        d = *(volatile unsigned long long *)P.done;
+        d = mcg_ld_relaxed(done);
       d = __shfl_sync(0xffffffffu, d, 0);
       if (d >= P.src_total)
         break;
-      if (*(volatile unsigned long long *)&P.counters[MCG_CNT_ERR] & 6ull)
-        break; /* a full ring, or a publication that never came */
-      const unsigned long long now = mcg_globaltimer();
+      if (errw & 30ull)
+        break; /* a full ring, or another warp gave up */
       if (d != seen_done || seen_t == 0) {
         seen_done = d;
         seen_t = now;
       } else if (now - seen_t > P.idle_limit_ns) {
-        timed_out = true;
+        stop = 4;
         break;
       }
-      __nanosleep(256);
+      __nanosleep(sleep_ns);
+      sleep_ns = min(sleep_ns * 2u, 32768u);
       continue;
     }
+    sleep_ns = 128;
     int dir = 0;
     bool finished = false;
     if (active) {
@@ -649,7 +717,7 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
         else if (idx == llo - 1)
           dir = L == 0 ? 0 : -1; /* the chain's ends leak (src/layer.cpp:47-48) */
         else if (idx == lhi)
-          dir = L == P.n_layers - 1 ? 0 : 1;
+          dir = L == nl - 1 ? 0 : 1;
         steps += nst;
         scat += nsc;
         finished = true;
@@ -658,8 +726,7 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
     }
     /* hand-over: one ticket atomic per destination ring and warp */
     const unsigned movers = __ballot_sync(0xffffffffu, finished && dir != 0);
-    if (finished && dir == 0)
-      ++n_done;
+    bool published = false;
     if (finished && dir != 0) {
       const int dst = L + dir;
       const unsigned peers = __match_any_sync(movers, dst);
@@ -677,22 +744,28 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
         o.seed = seed, o.x = x, o.mu = mu, o.wmc = wmc, o.index = idx + P.cell_lo;
         P.slots[s] = o;
         mcg_st_release(&P.seq[s], t + 1); /* publish */
+        published = true;
       }
       ++n_hand;
     }
-    /* finished histories count at once, so idle warps see progress */
-    unsigned long long fin = n_done;
-    for (int o = 16; o > 0; o >>= 1)
-      fin += __shfl_down_sync(0xffffffffu, fin, o);
-    if (lane == 0 && fin)
-      atomicAdd(P.done, fin);
-    n_done = 0;
-    /* a full ring ends the run for everyone */
-    if (*(volatile unsigned long long *)&P.counters[MCG_CNT_ERR] & 6ull)
-      break;
+    /* the published count and the finished histories, once per warp */
+    const unsigned npub = __popc(__ballot_sync(0xffffffffu, published));
+    const unsigned nfin = __popc(__ballot_sync(0xffffffffu, finished && dir == 0));
+    if (lane == 0) {
+      if (npub)
+        atomicAdd(reinterpret_cast<unsigned long long *>(pending), (unsigned long long)npub);
+      if (nfin)
+        atomicAdd(done, (unsigned long long)nfin);
+    }
   }
-  if (timed_out && lane == 0)
-    atomicOr(&P.counters[MCG_CNT_ERR], 4ull);
+  if (lane == 0) {
+    if (stop)
+      atomicOr(&P.counters[MCG_CNT_ERR], stop);
+    if (stop == 8)
+      atomicAdd(&P.state[MCG_AQ_DEADLINE_HITS], 1ull);
+    atomicMax(&P.state[MCG_AQ_ITERS], iters);
+    atomicAdd(&P.state[MCG_AQ_EXITED], 1ull);
+  }
   for (int o = 16; o > 0; o >>= 1) {
     n_hand += __shfl_down_sync(0xffffffffu, n_hand, o);
     steps += __shfl_down_sync(0xffffffffu, steps, o);
@@ -700,7 +773,7 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
   }
   if (lane == 0) {
     if (n_hand)
-      atomicAdd(P.handoffs, n_hand);
+      atomicAdd(&P.state[MCG_AQ_HANDOFFS], n_hand);
     atomicAdd(&P.counters[MCG_CNT_STEPS], steps);
     atomicAdd(&P.counters[MCG_CNT_SCAT], scat);
   }
@@ -754,11 +827,11 @@ extern "C" int mcg_worker_run_async(mcg_context *ctx, const mcg_source *src, int
   int rc = worker_buffer(ctx, o_slots + (size_t)P_ * cap * sizeof(mcg_particle), &wb);
   if (rc != MCG_OK)
     return rc;
-  unsigned long long *cnt = reinterpret_cast<unsigned long long *>(wb + o_c);
+  unsigned long long *state = reinterpret_cast<unsigned long long *>(wb + o_c);
   cudaError_t e;
   if ((e = cudaMemcpyAsync(wb + o_rings, rings.data(), P_ * sizeof(mcg_aq_ring),
                            cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess ||
-      (e = cudaMemsetAsync(cnt, 0, 64, ctx->stream)) != cudaSuccess)
+      (e = cudaMemsetAsync(state, 0, 256, ctx->stream)) != cudaSuccess)
     return mcg_cuda_fail(e, "mcg_worker_run_async: set-up");
   mcg_aq_init<<<ctx->sm_count * 4, 256, 0, ctx->stream>>>(
       reinterpret_cast<unsigned long long *>(wb + o_seq), (unsigned long long)P_ * cap, cap);
@@ -780,9 +853,7 @@ extern "C" int mcg_worker_run_async(mcg_context *ctx, const mcg_source *src, int
   A.slots = reinterpret_cast<mcg_particle *>(wb + o_slots);
   A.cap = cap;
   A.src = *src;
-  A.src_next = cnt;
-  A.done = cnt + 1;
-  A.handoffs = cnt + 2;
+  A.state = state;
   A.src_total = (unsigned long long)n;
   A.refill_steps = ctx->refill;
   A.min_w = ctx->min_w;
@@ -793,6 +864,9 @@ extern "C" int mcg_worker_run_async(mcg_context *ctx, const mcg_source *src, int
   A.libm_tab = ctx->libm_tab;
   A.max_steps = ctx->max_steps;
   A.idle_limit_ns = 2000000000ull; /* 2 s without any history finishing */
+  /* the launch's deadline: 30 s plus 2 us per history (the benchmark slab
+   * runs a history in about 40 ns of GPU time) */
+  A.budget_ns = 30000000000ull + 2000ull * (unsigned long long)n;
   auto kern = strict ? (use_smem ? mcg_worker_async<true, true> : mcg_worker_async<true, false>)
                      : (use_smem ? mcg_worker_async<false, true> : mcg_worker_async<false, false>);
   int bps = 1;
@@ -800,16 +874,57 @@ extern "C" int mcg_worker_run_async(mcg_context *ctx, const mcg_source *src, int
                                 ctx->smem_optin)) != cudaSuccess ||
       (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 1024, smem)) != cudaSuccess)
     return mcg_cuda_fail(e, "mcg_worker_run_async: launch set-up");
+  /* no more blocks than the histories need (idle warps only poll) */
+  const long long want = std::max<long long>(1, (n + 1023) / 1024);
+  const int grid = (int)std::min<long long>((long long)ctx->sm_count * std::max(bps, 1), want);
+  mcg_worker_state &WS = ctx->ext->worker;
+  if (!WS.monitor && (e = cudaStreamCreateWithFlags(&WS.monitor, cudaStreamNonBlocking)) != cudaSuccess)
+    return mcg_cuda_fail(e, "mcg_worker_run_async: monitor stream");
   cudaEventRecord(ctx->ev0, ctx->stream);
-  kern<<<ctx->sm_count * std::max(bps, 1), 1024, smem, ctx->stream>>>(A);
+  kern<<<grid, 1024, smem, ctx->stream>>>(A);
   e = cudaGetLastError();
   cudaEventRecord(ctx->ev1, ctx->stream);
   if (e != cudaSuccess)
     return mcg_cuda_fail(e, "mcg_worker_async launch");
   ctx->launches++;
-  unsigned long long host[3] = {0, 0, 0};
-  if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess ||
-      (e = cudaMemcpy(host, cnt, sizeof(host), cudaMemcpyDeviceToHost)) != cudaSuccess)
+  /* Host watchdog: the kernel stops itself at its deadline; if it has not
+   * ended 10 s after that, the host raises the abort word (read by every
+   * warp each round) from a second stream, and gives up 10 s later.  With
+   * MCG_WORKER_TRACE set, progress is printed to stderr every second. */
+  unsigned long long host[MCG_AQ_N] = {};
+  {
+    const bool trace = getenv("MCG_WORKER_TRACE") != nullptr;
+    const double limit_s = A.budget_ns * 1e-9 + 10.0;
+    const auto t0 = std::chrono::steady_clock::now();
+    double next_trace = 1.0;
+    bool aborted = false;
+    for (;;) {
+      e = cudaStreamQuery(ctx->stream);
+      if (e != cudaErrorNotReady)
+        break;
+      std::this_thread::sleep_for(std::chrono::milliseconds(2));
+      const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      if (trace && el >= next_trace) {
+        next_trace += 1.0;
+        if (cudaMemcpyAsync(host, state, sizeof(host), cudaMemcpyDeviceToHost, WS.monitor) == cudaSuccess &&
+            cudaStreamSynchronize(WS.monitor) == cudaSuccess)
+          fprintf(stderr, "worker_async %.1f s: done %llu born %llu pending %lld handoffs %llu "
+                  "warps exited %llu\n", el, host[MCG_AQ_DONE], host[MCG_AQ_SRC_NEXT],
+                  (long long)host[MCG_AQ_PENDING], host[MCG_AQ_HANDOFFS], host[MCG_AQ_EXITED]);
+      }
+      if (!aborted && el > limit_s) {
+        static const unsigned long long abort_word = 32ull;
+        cudaMemcpyAsync(state + MCG_AQ_ABORT, &abort_word, 8, cudaMemcpyHostToDevice, WS.monitor);
+        cudaStreamSynchronize(WS.monitor);
+        aborted = true;
+      }
+      if (el > limit_s + 10.0)
+        return mcg_fail(MCG_ERR_TIMEOUT, "mcg_worker_run_async: the launch did not stop after "
+                        "its deadline and an abort; the device context should be reset");
+    }
+  }
+  if (e != cudaSuccess ||
+      (e = cudaMemcpy(host, state, sizeof(host), cudaMemcpyDeviceToHost)) != cudaSuccess)
     return mcg_cuda_fail(e, "mcg_worker_run_async");
   cudaEventElapsedTime(&ctx->last_ms, ctx->ev0, ctx->ev1);
   unsigned long long err = 0;
@@ -818,15 +933,20 @@ extern "C" int mcg_worker_run_async(mcg_context *ctx, const mcg_source *src, int
   if (err & 2)
     return mcg_fail(MCG_ERR_OVERFLOW, "mcg_worker_run_async: a hand-over ring overflowed "
                     "(capacity %lld)", (long long)queue_capacity);
-  if (err & 4)
-    return mcg_fail(MCG_ERR_TIMEOUT, "mcg_worker_run_async: no history finished for %.1f s "
-                    "(%llu of %lld done)", A.idle_limit_ns * 1e-9, host[1], (long long)n);
+  if (err & 28)
+    return mcg_fail(MCG_ERR_TIMEOUT, "mcg_worker_run_async: %s (%llu of %lld histories done, "
+                    "%llu born, %lld published and unclaimed, %llu warps at the deadline)",
+                    (err & 8) ? "the launch's deadline passed"
+                    : (err & 16) ? "a published particle stayed invisible"
+                                 : "no history finished for 2 s",
+                    host[MCG_AQ_DONE], (long long)n, host[MCG_AQ_SRC_NEXT],
+                    (long long)host[MCG_AQ_PENDING], host[MCG_AQ_DEADLINE_HITS]);
   if (err & 1)
     return mcg_fail(MCG_ERR_LIMIT, "mcg_worker_run_async: a history exceeded the step limit");
   unsigned long long hcount = (unsigned long long)n;
   if ((e = cudaMemcpy(ctx->d_counters + MCG_CNT_HIST, &hcount, 8, cudaMemcpyHostToDevice)) != cudaSuccess)
     return mcg_cuda_fail(e, "mcg_worker_run_async: counters");
   if (h_handoffs)
-    *h_handoffs = (int64_t)host[2];
+    *h_handoffs = (int64_t)host[MCG_AQ_HANDOFFS];
   return MCG_OK;
 }
