@@ -217,13 +217,16 @@ int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n, int32_t p
  * warp takes particles from any sub-domain's ring (or newborns from the
  * source for the sub-domain holding src->cell0), simulates each inside its
  * sub-domain and appends leavers to the neighbour's ring, until all n
- * histories are finished.  A ring holding queue_capacity particles when
- * another arrives makes the call return MCG_ERR_OVERFLOW (the reference
- * aborts on a full buffer).  A warp takes queued particles before
- * newborns, so the rings together hold about as many particles as the GPU
- * has resident threads (SMs x 1024); twice that per ring is ample.  Warps
- * without work poll with short sleeps and give up with
- * MCG_ERR_TIMEOUT after 2 s in which no history finished.  Tallies and
+ * histories are finished.  Newborns are admitted only while fewer than
+ * queue_capacity - L histories are in flight (L = the launch's threads,
+ * at most SMs x 1024), which keeps every ring below queue_capacity: with a
+ * capacity of at least 2 L (3 L keeps every lane busy; queue_capacity 0
+ * selects 3 x SMs x 1024) no ring can overflow; with a smaller one a ring holding queue_capacity particles
+ * when another arrives makes the call return MCG_ERR_OVERFLOW (the
+ * reference aborts on a full buffer).  Warps without work poll with
+ * growing sleeps and give up with MCG_ERR_TIMEOUT after 2 s in which no
+ * history finished; every warp stops at the launch's deadline (30 s plus
+ * 2 us per history) with MCG_ERR_TIMEOUT, so the call always returns.  Tallies and
  * counters as the other entry points (equal to the fused tracker's);
  * *h_handoffs (may be NULL) counts the hand-overs.  The rings are kept in
  * the context between calls. */

@@ -413,14 +413,12 @@ class Context:
                                        int(queue_capacity), C.byref(cyc), C.byref(hand)))
         return cyc.value, hand.value
 
-    def worker_run_async(self, n, queue_capacity=None, seed_mode=0, base_seed=5127801, x0=0.0,
+    def worker_run_async(self, n, queue_capacity=0, seed_mode=0, base_seed=5127801, x0=0.0,
                          mu0=1.0, w0=1.0, isotropic=0, cell0=0):
         """The asynchronous workers (one persistent launch, bounded on-device
-        rings); returns the number of hand-overs.  The default capacity per
-        ring is twice the GPU's resident threads."""
-        if queue_capacity is None:
-            import torch
-            queue_capacity = 2048 * torch.cuda.get_device_properties(0).multi_processor_count
+        rings); returns the number of hand-overs.  queue_capacity 0: three
+        times the GPU's resident threads per ring, which admits twice the
+        resident threads in flight and can never overflow."""
         src = Source(seed_mode, isotropic, base_seed, x0, mu0, w0, cell0)
         hand = C.c_int64()
         _check(self.lib.mcg_worker_run_async(self.h, C.byref(src), int(n), int(queue_capacity),

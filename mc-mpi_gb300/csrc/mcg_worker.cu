@@ -452,7 +452,9 @@ extern "C" int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n
  * reading, frees the slots for the next lap (seq = t + C).  Nothing waits on
  * a slot: a producer that finds its slot still occupied (the ring holds C
  * particles) sets the overflow flag, as the reference aborts on a full
- * buffer.
+ * buffer.  Newborns are admitted only while fewer than `inflight` histories
+ * are born and unfinished, which bounds every ring's content: with a
+ * capacity of the grid's lanes plus `inflight` no ring can overflow.
  *
  * Idle warps must not crowd the rings: a global count of published,
  * unclaimed particles (a hint, exact once every producer and consumer has
@@ -496,6 +498,7 @@ struct mcg_async_params {
   const mcg_libm_tab *libm_tab;
   uint32_t max_steps;
   unsigned long long idle_limit_ns, budget_ns;
+  unsigned long long inflight; /* born and unfinished histories admitted */
 };
 
 __device__ __forceinline__ unsigned long long mcg_ld_acquire(const unsigned long long *p)
@@ -524,12 +527,25 @@ __device__ __forceinline__ unsigned long long mcg_globaltimer()
   return t;
 }
 
+/* The block's own ring in shared memory: a leaver goes there while the
+ * ring holds at most MCG_LQ - 1024 particles (then at most 1024 more can be
+ * reserved by the block's lanes at once, so it never overfills), else to the
+ * destination's global ring; idle lanes take from it first. */
+#define MCG_LQ 2048
+#define MCG_LQ_BYTES (16 + MCG_LQ * (4 + 4 + (int)sizeof(mcg_particle)))
+
 template <bool STRICT, bool SMEM>
 __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   mcg_libm_tab *T = reinterpret_cast<mcg_libm_tab *>(smem);
-  int2 *s_rng = reinterpret_cast<int2 *>(smem + sizeof(mcg_libm_tab)); /* [n_layers] lo, hi local */
+  /* local ring: head and tail tickets, publication words, sub-domain and
+   * particle of every slot */
+  unsigned *lq_ctl = reinterpret_cast<unsigned *>(smem + sizeof(mcg_libm_tab));
+  unsigned *lq_seq = lq_ctl + 4;
+  int *lq_L = reinterpret_cast<int *>(lq_seq + MCG_LQ);
+  mcg_particle *lq_part = reinterpret_cast<mcg_particle *>(lq_L + MCG_LQ);
+  int2 *s_rng = reinterpret_cast<int2 *>(smem + sizeof(mcg_libm_tab) + MCG_LQ_BYTES); /* [n_layers] lo, hi local */
   unsigned long long *s_tally =
       reinterpret_cast<unsigned long long *>(s_rng + ((P.n_layers + 1) & ~1));
   const int tid = threadIdx.x, lane = tid & 31;
@@ -542,6 +558,10 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
   if (SMEM)
     for (int i = tid; i < P.n_cells; i += blockDim.x)
       s_tally[i] = 0ull;
+  for (int i = tid; i < MCG_LQ; i += blockDim.x)
+    lq_seq[i] = (unsigned)i; /* free for its first-lap ticket */
+  if (tid < 4)
+    lq_ctl[tid] = 0u;
   __syncthreads();
   unsigned long long *tally = SMEM ? s_tally : P.tally;
   const float min_w = P.min_w;
@@ -570,6 +590,53 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
   for (;;) {
     unsigned need = __ballot_sync(0xffffffffu, !active);
     if (need) {
+      /* 0. the block's own hand-overs: claim the leading published run */
+      {
+        unsigned h = 0, e = 0;
+        if (lane == 0) {
+          h = *(volatile unsigned *)&lq_ctl[0];
+          e = *(volatile unsigned *)&lq_ctl[1];
+        }
+        h = __shfl_sync(0xffffffffu, h, 0);
+        e = __shfl_sync(0xffffffffu, e, 0);
+        if ((int)(e - h) > 0) {
+          const unsigned want = min((unsigned)__popc(need), e - h);
+          const bool pub = (unsigned)lane < want &&
+                           *(volatile unsigned *)&lq_seq[(h + lane) % MCG_LQ] == h + lane + 1u;
+          const unsigned pm = __ballot_sync(0xffffffffu, pub);
+          const int m = pm == 0xffffffffu ? 32 : __ffs(~pm) - 1;
+          if (m > 0) {
+            unsigned got = 0;
+            if (lane == 0)
+              got = atomicCAS(&lq_ctl[0], h, h + (unsigned)m);
+            got = __shfl_sync(0xffffffffu, got, 0);
+            if (got == h) {
+              const int rank = __popc(need & lanemask_lt());
+              if (((need >> lane) & 1u) && rank < m) {
+                const unsigned t = h + (unsigned)rank, sl = t % MCG_LQ;
+                int polls = 0;
+                while (*(volatile unsigned *)&lq_seq[sl] != t + 1u && ++polls < (1 << 16))
+                  ;
+                if (polls >= (1 << 16))
+                  atomicOr(&P.counters[MCG_CNT_ERR], 16ull);
+                __threadfence_block();
+                const mcg_particle q = lq_part[sl];
+                const int ql = lq_L[sl];
+                __threadfence_block();
+                *(volatile unsigned *)&lq_seq[sl] = t + (unsigned)MCG_LQ; /* next lap */
+                seed = q.seed, x = q.x, mu = q.mu, wmc = q.wmc, idx = q.index - P.cell_lo;
+                L = ql;
+                llo = s_rng[ql].x;
+                lhi = s_rng[ql].y;
+                inv_mu = mcg_flight_rcp(mu);
+                nst = nsc = 0;
+                active = true;
+              }
+              need = __ballot_sync(0xffffffffu, !active);
+            }
+          }
+        }
+      }
       /* 1. queued particles, when the published count says there are some:
        * each lane looks at one or two rings from this warp's rotating
        * start; the warp tries to claim a run of published tickets from at
@@ -637,12 +704,19 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
           need = __ballot_sync(0xffffffffu, !active);
         }
       }
-      /* 2. newborns from the source for the lanes still idle */
-      unsigned long long sn = 0;
-      if (lane == 0)
+      /* 2. newborns for the lanes still idle, while fewer than `inflight`
+       * histories are born and unfinished: every ring entry is such a
+       * history, and warps that pass this check together add at most 32
+       * each, so no ring ever holds more than inflight + the grid's lanes
+       * (the capacity the host sizes `inflight` from) */
+      unsigned long long sn = 0, dn = 0;
+      if (lane == 0) {
         sn = mcg_ld_relaxed(src_next);
+        dn = mcg_ld_relaxed(done);
+      }
       sn = __shfl_sync(0xffffffffu, sn, 0);
-      if (need && sn < P.src_total) {
+      dn = __shfl_sync(0xffffffffu, dn, 0);
+      if (need && sn < P.src_total && sn - dn < P.inflight) {
         unsigned long long base = 0;
         if (lane == 0)
           base = atomicAdd(src_next, (unsigned long long)__popc(need));
@@ -724,10 +798,46 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
         active = false;
       }
     }
-    /* hand-over: one ticket atomic per destination ring and warp */
+    /* hand-over: to the block's ring while it has room (one shared atomic
+     * per warp), else to the destination's global ring (one atomic per
+     * destination and warp) */
     const unsigned movers = __ballot_sync(0xffffffffu, finished && dir != 0);
     bool published = false;
-    if (finished && dir != 0) {
+    bool local = false;
+    if (movers) {
+      unsigned h = 0, e = 0;
+      if (lane == 0) {
+        h = *(volatile unsigned *)&lq_ctl[0];
+        e = *(volatile unsigned *)&lq_ctl[1];
+      }
+      h = __shfl_sync(0xffffffffu, h, 0);
+      e = __shfl_sync(0xffffffffu, e, 0);
+      local = e - h <= (unsigned)(MCG_LQ - 1024);
+    }
+    if (local && finished && dir != 0) {
+      const int leader = __ffs(movers) - 1;
+      unsigned base = 0;
+      if (lane == leader)
+        base = atomicAdd(&lq_ctl[1], (unsigned)__popc(movers));
+      base = __shfl_sync(movers, base, leader);
+      const unsigned t = base + __popc(movers & lanemask_lt()), sl = t % MCG_LQ;
+      /* the slot's previous occupant is claimed; its reader frees it at once */
+      int polls = 0;
+      while (*(volatile unsigned *)&lq_seq[sl] != t && ++polls < (1 << 16))
+        ;
+      if (polls >= (1 << 16)) {
+        atomicOr(&P.counters[MCG_CNT_ERR], 16ull);
+      } else {
+        mcg_particle o;
+        o.seed = seed, o.x = x, o.mu = mu, o.wmc = wmc, o.index = idx + P.cell_lo;
+        lq_part[sl] = o;
+        lq_L[sl] = L + dir;
+        __threadfence_block();
+        *(volatile unsigned *)&lq_seq[sl] = t + 1u; /* publish */
+      }
+      ++n_hand;
+    }
+    if (!local && finished && dir != 0) {
       const int dst = L + dir;
       const unsigned peers = __match_any_sync(movers, dst);
       const int leader = __ffs(peers) - 1;
@@ -796,8 +906,10 @@ __global__ void mcg_aq_init(unsigned long long *seq, unsigned long long total, u
 extern "C" int mcg_worker_run_async(mcg_context *ctx, const mcg_source *src, int64_t n,
                                     int64_t queue_capacity, int64_t *h_handoffs)
 {
-  if (!ctx || !src || n < 0 || queue_capacity <= 0)
+  if (!ctx || !src || n < 0 || queue_capacity < 0)
     return mcg_fail(MCG_ERR_ARG, "mcg_worker_run_async: bad arguments");
+  if (queue_capacity == 0) /* three times the resident threads: never overflows */
+    queue_capacity = 3LL * 1024 * ctx->sm_count;
   if (!ctx->d_tally)
     return mcg_fail(MCG_ERR_STATE, "mcg_worker_run_async: no layers set");
   cudaSetDevice(ctx->device);
@@ -836,7 +948,8 @@ extern "C" int mcg_worker_run_async(mcg_context *ctx, const mcg_source *src, int
   mcg_aq_init<<<ctx->sm_count * 4, 256, 0, ctx->stream>>>(
       reinterpret_cast<unsigned long long *>(wb + o_seq), (unsigned long long)P_ * cap, cap);
 
-  const size_t smem_base = sizeof(mcg_libm_tab) + (size_t)((P_ + 1) & ~1) * sizeof(int2);
+  const size_t smem_base =
+      sizeof(mcg_libm_tab) + MCG_LQ_BYTES + (size_t)((P_ + 1) & ~1) * sizeof(int2);
   const bool use_smem = smem_base + (size_t)ctx->n_cells * 8 <= (size_t)ctx->smem_optin;
   const size_t smem = smem_base + (use_smem ? (size_t)ctx->n_cells * 8 : 0);
   if (smem > (size_t)ctx->smem_optin)
@@ -877,6 +990,11 @@ extern "C" int mcg_worker_run_async(mcg_context *ctx, const mcg_source *src, int
   /* no more blocks than the histories need (idle warps only poll) */
   const long long want = std::max<long long>(1, (n + 1023) / 1024);
   const int grid = (int)std::min<long long>((long long)ctx->sm_count * std::max(bps, 1), want);
+  /* admission: a ring holds at most inflight + the grid's lanes particles,
+   * so capacity - lanes histories in flight can never overflow a ring (a
+   * smaller capacity still admits 32, and may overflow) */
+  const long long lanes = (long long)grid * 1024;
+  A.inflight = (unsigned long long)std::max<long long>(32, (long long)cap - lanes);
   mcg_worker_state &WS = ctx->ext->worker;
   if (!WS.monitor && (e = cudaStreamCreateWithFlags(&WS.monitor, cudaStreamNonBlocking)) != cudaSuccess)
     return mcg_cuda_fail(e, "mcg_worker_run_async: monitor stream");

@@ -114,9 +114,8 @@ void Worker::spin()
   int64_t cyc = 0, hand = 0;
   starttime = wall_seconds();
   if (async_) {
-    /* twice the resident threads of a GB300 (152 SMs x 1024) per ring */
-    if (mcg_worker_run_async(ctx_, &src, (int64_t)options.nb_particles, (int64_t)1 << 19,
-                             &hand) != MCG_OK)
+    /* the library's default ring capacity, which never overflows */
+    if (mcg_worker_run_async(ctx_, &src, (int64_t)options.nb_particles, 0, &hand) != MCG_OK)
       die("WorkerAsync::spin");
   } else {
     const int64_t cap = (int64_t)options.nb_particles + 1;

@@ -290,7 +290,14 @@ int orc_format_wa(const orc_layer *L, const float *tally_f32, char *buf, int cap
   return off;
 }
 
-/* ---- FP64 statistical restatement ---- */
+/* ---- FP64 statistical restatement ----
+ * The reference's problem (float cross sections, float cell faces
+ * (float)index * dx) with its physics evaluated in double: continuous
+ * flight samples h = s 2^-63, log and expm1 in double, double positions and
+ * weights.  The float faces matter: a face's rounding moves it by up to an
+ * ulp of x, which on a 10,000-cell slab changes a cell's width, hence its
+ * absorbed weight, by up to 2e-4 relative, about one standard error at 1e8
+ * histories. */
 void orc_fp64_histories(const orc_layer *layers, int n_layers, const float *sigs,
                         const float *rates, double min_w, const orc_particle *particles, int n,
                         double *tally, double *tally_sq_hist, double *leak, int nthreads)
@@ -337,8 +344,10 @@ void orc_fp64_histories(const orc_layer *layers, int n_layers, const float *sigs
         s = (RNG_G * s + RNG_C) & MASK63;
         double h = (double)s * 0x1p-63;
         double di = si > ORC_EPS ? -log(h) / si : DBL_MAX;
-        double dx = (double)L->dx;
-        double edge = mu < 0 ? idx * dx : (idx + 1) * dx;
+        /* the problem's cell faces are the reference's float values
+         * (float)index * dx (src/layer.cpp:146,150); only the physics runs
+         * in double */
+        double edge = mu < 0 ? (double)((float)idx * L->dx) : (double)((float)(idx + 1) * L->dx);
         double de = (mu < -ORC_EPS || ORC_EPS < mu) ? (edge - x) / mu : DBL_MAX;
         int nidx = mu < 0 ? idx - 1 : idx + 1;
         if (di < de) {
@@ -429,8 +438,8 @@ static int fp64_walk(const orc_layer *layers, int n_layers, const double *sa, co
     s = (RNG_G * s + RNG_C) & MASK63;
     double h = (double)s * 0x1p-63;
     double di = ss[idx] > ORC_EPS ? -log(h) / ss[idx] : DBL_MAX;
-    double dx = (double)L->dx;
-    double edge = mu < 0 ? idx * dx : (idx + 1) * dx;
+    /* the reference's float cell faces, as in orc_fp64_histories */
+    double edge = mu < 0 ? (double)((float)idx * L->dx) : (double)((float)(idx + 1) * L->dx);
     double de = (mu < -ORC_EPS || ORC_EPS < mu) ? (edge - x) / mu : DBL_MAX;
     int nidx = mu < 0 ? idx - 1 : idx + 1;
     int coll = di < de;

@@ -8,7 +8,8 @@ rnd_seed chain from 5127801 (histories 0 .. n-1, the source the GPU tests
 run through mcg_simulate_source), minimum weight 1e-12.
 
 The oracle's FP64 restatement of the physics (orc_fp64_histories: double
-arithmetic, log/expm1, the same LCG draws) runs every history; per cell it
+arithmetic, log/expm1, the same LCG draws, on the reference's float cell
+faces) runs every history; per cell it
 keeps the sum of the absorbed weight and the sum over histories of the
 square of each history's absorbed weight, so the per-cell standard error
 of the sum is exact.  Chunks of 1e6 histories are accumulated; a fixture is
