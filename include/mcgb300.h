@@ -218,9 +218,9 @@ int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n, int32_t p
  * source for the sub-domain holding src->cell0), simulates each inside its
  * sub-domain and appends leavers to the neighbour's ring, until all n
  * histories are finished.  Newborns are admitted only while fewer than
- * queue_capacity - L histories are in flight (L = the launch's threads,
- * at most SMs x 1024), which keeps every ring below queue_capacity: with a
- * capacity of at least 2 L (3 L keeps every lane busy; queue_capacity 0
+ * min(queue_capacity - L, 1.125 L) histories are in flight (L = the
+ * launch's threads, at most SMs x 1024), which keeps every ring below
+ * queue_capacity: with a capacity of at least 2 L (queue_capacity 0
  * selects 3 x SMs x 1024) no ring can overflow; with a smaller one a ring holding queue_capacity particles
  * when another arrives makes the call return MCG_ERR_OVERFLOW (the
  * reference aborts on a full buffer).  Warps without work poll with

@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
     /* lanes refill from the item's histories [0, it.count) */
     uint64_t seed = 0;
     float x = 0.f, mu = 0.f, wmc = 0.f, inv_mu = 0.f;
+    float wres = 0.f; /* fast: the weight's rounding residue */
     int idx = 0;
     uint32_t nst = 0, nsc = 0;
     bool active = false;
@@ -143,6 +144,7 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
         if (!active && my >= 0) {
           mcg_source_particle(S, it.first + my, seed, x, mu, wmc, idx);
           inv_mu = mcg_flight_rcp(mu);
+          wres = 0.f;
           nst = nsc = 0;
           active = true;
         }
@@ -161,7 +163,9 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
           bool rest = false;
           while ((k < kmax) & (wmc >= min_w) & ((unsigned)idx < (unsigned)m)) {
             if (!mcg_step_cross<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx,
-                                               __ldg(cells + idx), &tally[idx], qs, T, P.libm)) {
+                                               __ldg(cells + idx), &tally[idx], qs, T, P.libm,
+                                               nullptr, nullptr, nullptr,
+                                               STRICT ? nullptr : &wres)) {
               rest = true;
               break;
             }
@@ -169,13 +173,15 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
           }
           if (rest) {
             mcg_step_rest<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(cells + idx),
-                                         &tally[idx], qs, T, P.libm);
+                                         &tally[idx], qs, T, P.libm, nullptr, nullptr, nullptr,
+                                         STRICT ? nullptr : &wres);
             ++k;
           }
         } else {
           while ((k < kmax) & (wmc >= min_w) & ((unsigned)idx < (unsigned)m)) {
             mcg_step<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(cells + idx),
-                                    &tally[idx], qs, T, P.libm);
+                                    &tally[idx], qs, T, P.libm, nullptr, nullptr, nullptr,
+                                    STRICT ? nullptr : &wres);
             ++k;
           }
         }
@@ -196,7 +202,8 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
           else
             r = -1;
           atomicAdd(&s_cnt[MCG_CNT_HIST], 1ull);
-          const unsigned long long wq = (unsigned long long)mcg_to_fixed(wmc, qs);
+          const unsigned long long wq =
+              (unsigned long long)(mcg_to_fixed(wmc, qs) + (STRICT ? 0ll : mcg_to_fixed(wres, qs)));
           if (r == -1) {
             atomicAdd(&s_cnt[MCG_CNT_LEFT], 1ull);
             atomicAdd(&s_cnt[MCG_CNT_WLEFT], wq);

@@ -27,7 +27,7 @@
  *
  * The engine serves one chain (mcg_set_algorithm) and the batched slabs
  * (mcg_batch_set_algorithm; the bank then carries the slab index).
- * Memory per particle and pass: 36 B read + 36 B written (+ 36 B each way
+ * Memory per particle and pass: 40 B read + 40 B written (+ 40 B each way
  * through the queue for a collision).
  */
 #include <algorithm>
@@ -66,7 +66,7 @@ struct mcg_ev_params {
 /* A lane's particle. */
 struct mcg_ev_particle {
   uint64_t seed;
-  float x, mu, wmc;
+  float x, mu, wmc, res; /* res: the fast weight's rounding residue */
   int32_t idx, hid, nst, nsc;
 };
 
@@ -77,6 +77,7 @@ __device__ __forceinline__ void mcg_ev_store(const mcg_soa &b, unsigned long lon
   b.x[i] = p.x;
   b.mu[i] = p.mu;
   b.wmc[i] = p.wmc;
+  b.res[i] = p.res;
   b.idx[i] = p.idx;
   b.hid[i] = p.hid;
   b.nst[i] = p.nst;
@@ -95,6 +96,7 @@ __device__ __forceinline__ void mcg_ev_load4(const mcg_soa &b, unsigned long lon
     const float4 vx = reinterpret_cast<const float4 *>(b.x)[q];
     const float4 vm = reinterpret_cast<const float4 *>(b.mu)[q];
     const float4 vw = reinterpret_cast<const float4 *>(b.wmc)[q];
+    const float4 vr = reinterpret_cast<const float4 *>(b.res)[q];
     const int4 vi = reinterpret_cast<const int4 *>(b.idx)[q];
     const int4 vh = reinterpret_cast<const int4 *>(b.hid)[q];
     const int4 vs = reinterpret_cast<const int4 *>(b.nst)[q];
@@ -103,6 +105,7 @@ __device__ __forceinline__ void mcg_ev_load4(const mcg_soa &b, unsigned long lon
     p[0].x = vx.x, p[1].x = vx.y, p[2].x = vx.z, p[3].x = vx.w;
     p[0].mu = vm.x, p[1].mu = vm.y, p[2].mu = vm.z, p[3].mu = vm.w;
     p[0].wmc = vw.x, p[1].wmc = vw.y, p[2].wmc = vw.z, p[3].wmc = vw.w;
+    p[0].res = vr.x, p[1].res = vr.y, p[2].res = vr.z, p[3].res = vr.w;
     p[0].idx = vi.x, p[1].idx = vi.y, p[2].idx = vi.z, p[3].idx = vi.w;
     p[0].hid = vh.x, p[1].hid = vh.y, p[2].hid = vh.z, p[3].hid = vh.w;
     p[0].nst = vs.x, p[1].nst = vs.y, p[2].nst = vs.z, p[3].nst = vs.w;
@@ -120,6 +123,7 @@ __device__ __forceinline__ void mcg_ev_load4(const mcg_soa &b, unsigned long lon
         p[j].x = b.x[i];
         p[j].mu = b.mu[i];
         p[j].wmc = b.wmc[i];
+        p[j].res = b.res[i];
         p[j].idx = b.idx[i];
         p[j].hid = b.hid[i];
         p[j].nst = b.nst[i];
@@ -173,7 +177,9 @@ __device__ __forceinline__ void mcg_ev_finish(const mcg_ev_params &P, const mcg_
       P.tp.scatters[h] = p.nsc;
   }
   atomicAdd(&s_cnt[MCG_CNT_HIST], 1ull);
-  const unsigned long long wq = (unsigned long long)mcg_to_fixed(p.wmc, P.q_log2);
+  /* the weight with its rounding residue (zero in strict mode) */
+  const unsigned long long wq =
+      (unsigned long long)(mcg_to_fixed(p.wmc, P.q_log2) + mcg_to_fixed(p.res, P.q_log2));
   if (r == -1) {
     atomicAdd(&s_cnt[MCG_CNT_LEFT], 1ull);
     atomicAdd(&s_cnt[MCG_CNT_WLEFT], wq);
@@ -286,7 +292,9 @@ __global__ void __launch_bounds__(MCG_EV_BLOCK, MCG_EV_MIN_BLOCKS) mcg_ev_flight
         }
         if (!mcg_step_cross<STRICT, SMEM ? MCG_TALLY_SMEM32 : MCG_TALLY_GLOBAL>(p[j].seed, p[j].x, p[j].mu, p[j].wmc,
                                                       inv_mu, p[j].idx, __ldg(cells + p[j].idx),
-                                                      &tally[p[j].idx], P.q_log2, &T, P.libm)) {
+                                                      &tally[p[j].idx], P.q_log2, &T, P.libm,
+                                                      nullptr, nullptr, nullptr,
+                                                      STRICT ? nullptr : &p[j].res)) {
           queued[j] = true;
           break;
         }
@@ -354,7 +362,9 @@ __global__ void __launch_bounds__(MCG_EV_BLOCK, MCG_EV_MIN_BLOCKS) mcg_ev_collid
       uint32_t sc = (uint32_t)p[j].nsc;
       mcg_step_rest<STRICT, SMEM ? MCG_TALLY_SMEM32 : MCG_TALLY_GLOBAL>(p[j].seed, p[j].x, p[j].mu, p[j].wmc, inv_mu,
                                               p[j].idx, sc, __ldg(cells + p[j].idx),
-                                              &tally[p[j].idx], P.q_log2, &T, P.libm);
+                                              &tally[p[j].idx], P.q_log2, &T, P.libm,
+                                              nullptr, nullptr, nullptr,
+                                              STRICT ? nullptr : &p[j].res);
       scat += sc - (uint32_t)p[j].nsc;
       p[j].nsc = (int)sc;
       ++p[j].nst;
@@ -421,6 +431,7 @@ __global__ void mcg_ev_birth_kernel(mcg_ev_params P)
     }
     p.idx = idx;
     p.nst = p.nsc = 0;
+    p.res = 0.f;
     mcg_ev_store(P.out, base + i, p);
   }
 }
@@ -452,6 +463,7 @@ __global__ void __launch_bounds__(MCG_EV_BLOCK, MCG_EV_MIN_BLOCKS) mcg_ev_drain_
     p.x = P.in.x[i];
     p.mu = P.in.mu[i];
     p.wmc = P.in.wmc[i];
+    p.res = P.in.res[i];
     p.idx = P.in.idx[i];
     p.hid = P.in.hid[i];
     p.nst = P.in.nst[i];
@@ -469,7 +481,8 @@ __global__ void __launch_bounds__(MCG_EV_BLOCK, MCG_EV_MIN_BLOCKS) mcg_ev_drain_
       mcg_step<STRICT, SMEM ? MCG_TALLY_SMEM32 : MCG_TALLY_GLOBAL>(p.seed, p.x, p.mu, p.wmc,
                                                                   inv_mu, p.idx, sc,
                                          __ldg(cells + p.idx), &tally[p.idx], P.q_log2, &T,
-                                         P.libm);
+                                         P.libm, nullptr, nullptr, nullptr,
+                                         STRICT ? nullptr : &p.res);
       ++st;
     }
     steps += st - st0;
@@ -489,14 +502,14 @@ static int soa_alloc(mcg_soa &s, size_t cap, std::vector<void *> &owned)
   void *base = nullptr;
   /* one allocation, each field 256-byte aligned (128-bit loads of quads) */
   const size_t pad = (cap + 63) & ~(size_t)63;
-  cudaError_t e = cudaMalloc(&base, pad * (8 + 7 * 4));
+  cudaError_t e = cudaMalloc(&base, pad * (8 + 8 * 4));
   if (e != cudaSuccess)
     return mcg_cuda_fail(e, "event buffers");
   owned.push_back(base);
   char *p = static_cast<char *>(base);
   s.seed = reinterpret_cast<unsigned long long *>(p);
   p += pad * 8;
-  float **f[3] = {&s.x, &s.mu, &s.wmc};
+  float **f[4] = {&s.x, &s.mu, &s.wmc, &s.res};
   for (float **q : f) {
     *q = reinterpret_cast<float *>(p);
     p += pad * 4;

@@ -74,7 +74,7 @@ struct mcg_ext {
  * sample's state, which determines the sample. */
 struct mcg_soa {
   unsigned long long *seed;
-  float *x, *mu, *wmc;
+  float *x, *mu, *wmc, *res; /* res: the fast weight's rounding residue */
   int32_t *idx, *hid, *nst, *nsc;
 };
 

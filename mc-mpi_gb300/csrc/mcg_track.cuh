@@ -138,6 +138,19 @@ __device__ __forceinline__ void mcg_load_particle(const mcg_track_params &P, int
   }
 }
 
+/* The fast arithmetic's weight update wmc <- RN(wmc - dep), with the exact
+ * rounding residue (Fast2Sum: |dep| <= |wmc|) added to *wres when given: the
+ * particle's weight is then the pair wmc + wres, so deposits plus final
+ * weights conserve the born weight, while each deposit stays the rounded
+ * product om wmc (no per-cell bias). */
+__device__ __forceinline__ void mcg_fast_weight_update(float &wmc, float dep, float *wres)
+{
+  const float w = __fsub_rn(wmc, dep);
+  if (wres)
+    *wres = __fadd_rn(*wres, __fsub_rn(__fsub_rn(wmc, w), dep));
+  wmc = w;
+}
+
 /* The fast step's flight: the crossing's absorption 1 - e^(-sig_a de) into
  * om_cross, and whether the flight ends in a collision before the face, the
  * event -ln(1 - u) / sig_i < de of the reference's test evaluated as
@@ -180,7 +193,8 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
                                          unsigned long long *tally_cell, int qs,
                                          const mcg_libm_tab *T, const mcg_libm_dev &LM,
                                          float *l_out = nullptr,
-                                         bool *coll_out = nullptr, float *dep_out = nullptr)
+                                         bool *coll_out = nullptr, float *dep_out = nullptr,
+                                         float *wres = nullptr)
 {
   const float sig_a = c.x;
   mcg_lcg_next(seed); /* the flight sample's state */
@@ -277,7 +291,7 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
                       (__float_as_uint(v_q) < 0x4f000000u);
     if (easy) {
       x = edge;
-      wmc = __fsub_rn(wmc, dep_q);
+      mcg_fast_weight_update(wmc, dep_q, wres);
       if (tally_cell)
         mcg_deposit_u31<TALLY>(tally_cell, v_q);
       if (l_out) {
@@ -314,7 +328,7 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
      * (om ~ 1e-5) is a 3e-3 relative error of the deposit, the same for
      * every uncollided particle of a cell: a systematic per-cell bias */
     const float dep = __fmul_rn(om, wmc);
-    wmc = __fsub_rn(wmc, dep);
+    mcg_fast_weight_update(wmc, dep, wres);
     if (tally_cell)
       mcg_deposit<TALLY>(tally_cell, dep, qs);
     if (dep_out)
@@ -344,7 +358,8 @@ __device__ __forceinline__ bool mcg_step_cross(uint64_t &seed, float &x, float &
                                                unsigned long long *tally_cell, int qs,
                                                const mcg_libm_tab *T, const mcg_libm_dev &LM,
                                                float *l_out = nullptr,
-                                               bool *coll_out = nullptr, float *dep_out = nullptr)
+                                               bool *coll_out = nullptr, float *dep_out = nullptr,
+                                               float *wres = nullptr)
 {
   const float sig_a = c.x;
   mcg_lcg_next(seed); /* the flight sample's state */
@@ -395,7 +410,7 @@ __device__ __forceinline__ bool mcg_step_cross(uint64_t &seed, float &x, float &
      * (om ~ 1e-5) is a 3e-3 relative error of the deposit, the same for
      * every uncollided particle of a cell: a systematic per-cell bias */
     const float dep = __fmul_rn(om, wmc);
-    wmc = __fsub_rn(wmc, dep);
+    mcg_fast_weight_update(wmc, dep, wres);
     if (tally_cell)
       mcg_deposit<TALLY>(tally_cell, dep, qs);
     if (dep_out)
@@ -411,7 +426,8 @@ __device__ __forceinline__ void mcg_step_rest(uint64_t &seed, float &x, float &m
                                               const float4 c, unsigned long long *tally_cell,
                                               int qs, const mcg_libm_tab *T,
                                               const mcg_libm_dev &LM, float *l_out = nullptr,
-                                              bool *coll_out = nullptr, float *dep_out = nullptr)
+                                              bool *coll_out = nullptr, float *dep_out = nullptr,
+                                              float *wres = nullptr)
 {
   const float sig_a = c.x;
   const bool neg = mu < 0.0f;
@@ -480,7 +496,7 @@ __device__ __forceinline__ void mcg_step_rest(uint64_t &seed, float &x, float &m
       om = om_cross;
     }
     const float dep = __fmul_rn(om, wmc);
-    wmc = __fsub_rn(wmc, dep);
+    mcg_fast_weight_update(wmc, dep, wres);
     if (tally_cell)
       mcg_deposit<TALLY>(tally_cell, dep, qs);
     if (dep_out)
@@ -517,6 +533,7 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
 
   uint64_t seed = 0;
   float x = 0.f, mu = 0.f, wmc = 0.f, inv_mu = 0.f;
+  float wres = 0.f; /* fast: the weight's rounding residue (mcg_fast_weight_update) */
   int idx = 0;
   int64_t hid = -1;
   uint32_t nst = 0, nsc = 0;
@@ -558,6 +575,7 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
         mcg_load_particle(P, hid, seed, x, mu, wmc, idx);
         idx -= lo;
         inv_mu = mcg_flight_rcp(mu);
+        wres = 0.f;
         nst = nsc = 0;
         active = true;
       }
@@ -573,7 +591,8 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
       int k = 0;
       while ((k < kmax) & (wmc >= min_w) & ((unsigned)idx < (unsigned)ncell)) {
         mcg_step<STRICT, TALLY, THIN>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + idx),
-                                      &my_tally[idx], qs, T, P.libm);
+                                      &my_tally[idx], qs, T, P.libm, nullptr, nullptr, nullptr,
+                                      STRICT ? nullptr : &wres);
         ++k;
       }
       const bool going = (wmc >= min_w) & ((unsigned)idx < (unsigned)ncell);
@@ -609,6 +628,8 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
           P.scatters[hid] = nsc;
         atomicAdd(&s_cnt[MCG_CNT_HIST], 1ull);
         long long wq = mcg_to_fixed(wmc, qs);
+        if (!STRICT)
+          wq += mcg_to_fixed(wres, qs); /* the weight's float-float remainder */
         if (r == -1) {
           atomicAdd(&s_cnt[MCG_CNT_LEFT], 1ull);
           atomicAdd(&s_cnt[MCG_CNT_WLEFT], (unsigned long long)wq);

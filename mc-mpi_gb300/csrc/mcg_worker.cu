@@ -736,13 +736,20 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
       scan = (scan + 1) % nl;
     }
     ++iters;
+    /* the deadline, the abort word and the error word: every 32 rounds of a
+     * busy warp (three global reads), every round of an idle one */
+    const bool idle = !__any_sync(0xffffffffu, active);
     unsigned long long now = 0, errw = 0;
-    if (lane == 0) {
-      now = mcg_globaltimer();
-      errw = mcg_ld_relaxed(&P.counters[MCG_CNT_ERR]) | mcg_ld_relaxed(&P.state[MCG_AQ_ABORT]);
+    if (idle || (iters & 31u) == 0) {
+      if (lane == 0) {
+        now = mcg_globaltimer();
+        errw = mcg_ld_relaxed(&P.counters[MCG_CNT_ERR]) | mcg_ld_relaxed(&P.state[MCG_AQ_ABORT]);
+      }
+      now = __shfl_sync(0xffffffffu, now, 0);
+      errw = __shfl_sync(0xffffffffu, errw, 0);
+    } else {
+      now = t_start;
     }
-    now = __shfl_sync(0xffffffffu, now, 0);
-    errw = __shfl_sync(0xffffffffu, errw, 0);
     if (now - t_start > P.budget_ns || (errw & 32ull)) {
       /* the launch's deadline, or the host's abort: abandon what this warp
        * holds */
@@ -751,7 +758,7 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
     }
     if (errw & 30ull)
       break; /* a full ring, or another warp gave up */
-    if (!__any_sync(0xffffffffu, active)) {
+    if (idle) {
       /* nothing to do: finished, or wait (backing off) for hand-overs */
       unsigned long long d = 0;
       if (lane == 0)
@@ -994,7 +1001,11 @@ extern "C" int mcg_worker_run_async(mcg_context *ctx, const mcg_source *src, int
    * so capacity - lanes histories in flight can never overflow a ring (a
    * smaller capacity still admits 32, and may overflow) */
   const long long lanes = (long long)grid * 1024;
-  A.inflight = (unsigned long long)std::max<long long>(32, (long long)cap - lanes);
+  /* about one history per lane plus an eighth in transit: more would only
+   * wait in the rings (and spill from the blocks' own rings to the global
+   * ones) */
+  A.inflight = (unsigned long long)std::max<long long>(
+      32, std::min<long long>((long long)cap - lanes, lanes + lanes / 8));
   mcg_worker_state &WS = ctx->ext->worker;
   if (!WS.monitor && (e = cudaStreamCreateWithFlags(&WS.monitor, cudaStreamNonBlocking)) != cudaSuccess)
     return mcg_cuda_fail(e, "mcg_worker_run_async: monitor stream");
