@@ -584,11 +584,6 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
   const unsigned long long t_start = __shfl_sync(0xffffffffu, mcg_globaltimer(), 0);
   unsigned long long iters = 0;
   int scan = gwarp % nl;
-  /* the published count, the source index and the finished count, read by
-   * lane 0 at the end of every round for the next one's acquisition, so the
-   * reads' latency overlaps the round's steps (they are hints: a value one
-   * round old changes no bound below) */
-  unsigned long long pf_pend = 0, pf_sn = 0, pf_dn = 0;
   unsigned sleep_ns = 128;
   unsigned long long stop = 0; /* 4: idle limit, 8: deadline */
 
@@ -646,7 +641,10 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
        * each lane looks at one or two rings from this warp's rotating
        * start; the warp tries to claim a run of published tickets from at
        * most four of the non-empty ones */
-      const long long pend = (long long)__shfl_sync(0xffffffffu, pf_pend, 0);
+      long long pend = 0;
+      if (lane == 0)
+        pend = (long long)mcg_ld_relaxed(reinterpret_cast<unsigned long long *>(pending));
+      pend = __shfl_sync(0xffffffffu, pend, 0);
       if (pend > 0) {
         const int r0 = (scan + lane) % nl, r1 = (scan + lane + 32) % nl;
         const bool ne0 = lane < nl && mcg_ld_relaxed(&P.rings[r0].enq) > mcg_ld_relaxed(&P.rings[r0].deq);
@@ -711,8 +709,13 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
        * history, and warps that pass this check together add at most 32
        * each, so no ring ever holds more than inflight + the grid's lanes
        * (the capacity the host sizes `inflight` from) */
-      const unsigned long long sn = __shfl_sync(0xffffffffu, pf_sn, 0);
-      const unsigned long long dn = __shfl_sync(0xffffffffu, pf_dn, 0);
+      unsigned long long sn = 0, dn = 0;
+      if (lane == 0) {
+        sn = mcg_ld_relaxed(src_next);
+        dn = mcg_ld_relaxed(done);
+      }
+      sn = __shfl_sync(0xffffffffu, sn, 0);
+      dn = __shfl_sync(0xffffffffu, dn, 0);
       if (need && sn < P.src_total && sn - dn < P.inflight) {
         unsigned long long base = 0;
         if (lane == 0)
@@ -758,12 +761,8 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
     if (idle) {
       /* nothing to do: finished, or wait (backing off) for hand-overs */
       unsigned long long d = 0;
-      if (lane == 0) {
+      if (lane == 0)
         d = mcg_ld_relaxed(done);
-        pf_pend = mcg_ld_relaxed(reinterpret_cast<unsigned long long *>(pending));
-        pf_sn = mcg_ld_relaxed(src_next);
-        pf_dn = d;
-      }
       d = __shfl_sync(0xffffffffu, d, 0);
       if (d >= P.src_total)
         break;
@@ -805,11 +804,6 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
         finished = true;
         active = false;
       }
-    }
-    if (lane == 0) {
-      pf_pend = mcg_ld_relaxed(reinterpret_cast<unsigned long long *>(pending));
-      pf_sn = mcg_ld_relaxed(src_next);
-      pf_dn = mcg_ld_relaxed(done);
     }
     /* hand-over: to the block's ring while it has room (one shared atomic
      * per warp), else to the destination's global ring (one atomic per
