@@ -267,11 +267,13 @@ int mcg_batch_tally_read(mcg_context *ctx, int64_t *h_q, double *h_f64);
  * (as mcg_set_tally_mode). 0 keeps the current value. */
 int mcg_batch_set_launch(mcg_context *ctx, int32_t block, int64_t item_histories,
                          int32_t tally_mode);
-/* Deferral of the full step in mcg_batch_run (0 off, the default; 1 on):
- * a lane whose step is not a certain crossing stops stepping for the rest
- * of its refill round, and the warp's stopped lanes complete their steps
- * together at the round's end, instead of the warp running the full step
- * once for every step any of its lanes needs it.  Same results. */
+/* Deferral of the full step in mcg_batch_run (0 off, the default; 1..32
+ * on): a lane whose step is not a certain crossing waits while the warp's
+ * other lanes keep crossing, and the waiting lanes complete their steps
+ * together once at least `defer` of them wait (or no other lane can step),
+ * instead of the warp running the full step once for every step any of its
+ * lanes needs it; lanes refill when two have ended their histories.  Same
+ * results for every value. */
 int mcg_batch_set_deferral(mcg_context *ctx, int32_t defer);
 /* Autotuner: times every candidate on a sample of each slab's histories
  * (fraction in (0, 1], raised so that the sample holds at least four times
@@ -288,7 +290,7 @@ typedef struct mcg_batch_tuning {
   int32_t candidates;
   int32_t algorithm;      /* MCG_ALGO_HISTORY or MCG_ALGO_EVENT */
   int32_t steps_per_pass; /* event mode: events per pass */
-  int32_t defer;          /* history mode: deferral of the full step (0/1) */
+  int32_t defer;          /* history mode: waiting lanes of the deferred full step, 0 off */
 } mcg_batch_tuning;
 int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_batch_tuning *out);
 

@@ -392,7 +392,9 @@ class Context:
         _check(self.lib.mcg_batch_set_launch(self.h, block, item_histories, tally_mode))
 
     def batch_set_deferral(self, defer):
-        _check(self.lib.mcg_batch_set_deferral(self.h, 1 if defer else 0))
+        """0/False: off; True: 8 waiting lanes; 1..32: that many."""
+        lanes = 8 if defer is True else int(defer)
+        _check(self.lib.mcg_batch_set_deferral(self.h, lanes))
 
     def batch_set_algorithm(self, algorithm="history", steps_per_pass=0):
         _check(self.lib.mcg_batch_set_algorithm(self.h, 0 if algorithm == "history" else 1,

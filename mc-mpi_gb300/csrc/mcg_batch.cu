@@ -50,7 +50,13 @@ struct mcg_batch_params {
   int32_t q_log2;
   int32_t refill_steps;
   uint32_t max_steps;
+  int32_t defer_lanes; /* DEFER: waiting lanes that trigger the full steps */
 };
+
+/* DEFER: certain crossings a lane takes between two of the warp's checks,
+ * and the idle lanes (history ended) at which the warp refills */
+#define MCG_DEFER_WINDOW 4
+#define MCG_DEFER_REFILL 2
 
 template <bool STRICT, int TALLY, bool DEFER>
 __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
@@ -113,6 +119,7 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
     int idx = 0;
     uint32_t nst = 0, nsc = 0;
     bool active = false;
+    bool wait = false; /* DEFER: the lane's step waits for the full step */
     long long pool_next = 0, pool_end = 0;
     bool drained = false;
     for (;;) {
@@ -151,42 +158,67 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
       }
       if (!__any_sync(0xffffffffu, active))
         break;
-      if (active) {
-        /* up to refill_steps steps, never past the step limit; one
-         * unsigned compare is the slab's range test */
-        const int kmax = (int)min((uint32_t)P.refill_steps, P.max_steps - nst);
-        int k = 0;
-        if (DEFER) {
-          /* certain crossings only; a lane whose step is anything else stops
-           * here, and the warp's stopped lanes complete their steps together
-           * below (mcg_step_cross + mcg_step_rest perform exactly mcg_step) */
-          bool rest = false;
-          while ((k < kmax) & (wmc >= min_w) & ((unsigned)idx < (unsigned)m)) {
+      int k = 0;
+      if (DEFER) {
+        /* pooled deferral, run by the whole warp: a lane whose step is not
+         * a certain crossing waits (mcg_step_cross has advanced only its
+         * seed) while the others keep crossing, and the waiting lanes
+         * complete their steps together (mcg_step_rest) once defer_lanes of
+         * them wait or no other lane can step, so the long full step runs
+         * with many lanes instead of once for every lane that needs it.
+         * The round lasts until MCG_DEFER_REFILL lanes have ended their
+         * histories (while the item has more) or no lane can step; a lane
+         * may still wait when it ends, and its step completes in a later
+         * round.  mcg_step_cross + mcg_step_rest perform exactly mcg_step
+         * and each lane's steps keep their order: same results.  Every pass
+         * steps a lane, makes one wait or completes the waiting steps, and
+         * no lane passes its step limit, so the round ends. */
+        const uint32_t kcap = active ? P.max_steps - nst : 0u;
+        for (;;) {
+          bool go = !wait & ((uint32_t)k < kcap) & (wmc >= min_w) & ((unsigned)idx < (unsigned)m);
+          for (int j = 0; go & (j < MCG_DEFER_WINDOW); ++j) {
             if (!mcg_step_cross<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx,
                                                __ldg(cells + idx), &tally[idx], qs, T, P.libm,
                                                nullptr, nullptr, nullptr,
                                                STRICT ? nullptr : &wres)) {
-              rest = true;
+              wait = true;
               break;
             }
             ++k;
+            go = ((uint32_t)k < kcap) & (wmc >= min_w) & ((unsigned)idx < (unsigned)m);
           }
-          if (rest) {
-            mcg_step_rest<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(cells + idx),
-                                         &tally[idx], qs, T, P.libm, nullptr, nullptr, nullptr,
-                                         STRICT ? nullptr : &wres);
-            ++k;
-          }
-        } else {
-          while ((k < kmax) & (wmc >= min_w) & ((unsigned)idx < (unsigned)m)) {
-            mcg_step<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(cells + idx),
-                                    &tally[idx], qs, T, P.libm, nullptr, nullptr, nullptr,
-                                    STRICT ? nullptr : &wres);
-            ++k;
+          go &= !wait;
+          const unsigned wb = __ballot_sync(0xffffffffu, wait);
+          const unsigned gb = __ballot_sync(0xffffffffu, go);
+          if (!wb && !gb)
+            break;
+          if (wb && (!gb || __popc(wb) >= P.defer_lanes)) {
+            if (wait) {
+              mcg_step_rest<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc,
+                                           __ldg(cells + idx), &tally[idx], qs, T, P.libm,
+                                           nullptr, nullptr, nullptr, STRICT ? nullptr : &wres);
+              ++k;
+              wait = false;
+            }
+          } else if (!drained && __popc(~(wb | gb)) >= MCG_DEFER_REFILL) {
+            break;
           }
         }
-        const bool going = (wmc >= min_w) & ((unsigned)idx < (unsigned)m);
+      } else if (active) {
+        /* up to refill_steps steps, never past the step limit; one
+         * unsigned compare is the slab's range test */
+        const int kmax = (int)min((uint32_t)P.refill_steps, P.max_steps - nst);
+        while ((k < kmax) & (wmc >= min_w) & ((unsigned)idx < (unsigned)m)) {
+          mcg_step<STRICT, TALLY>(seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(cells + idx),
+                                  &tally[idx], qs, T, P.libm, nullptr, nullptr, nullptr,
+                                  STRICT ? nullptr : &wres);
+          ++k;
+        }
+      }
+      if (active)
         nst += (uint32_t)k;
+      if (active && !wait) {
+        const bool going = (wmc >= min_w) & ((unsigned)idx < (unsigned)m);
         if (!going || nst >= P.max_steps) {
           /* a history still alive in the slab here has reached the limit */
           const bool in = (wmc >= min_w) && ((unsigned)idx < (unsigned)m);
@@ -312,7 +344,7 @@ extern "C" int mcg_batch_set(mcg_context *ctx, int32_t n_slabs, const mcg_slab *
   cudaStreamSynchronize(ctx->stream);
   mcg_batch_state *B = batch_of(ctx);
   const int keep_block = B->block, keep_tm = B->tally_mode;
-  const bool keep_defer = B->defer;
+  const int keep_defer = B->defer;
   const int64_t keep_item = B->item_histories;
   batch_free(B);
   B->block = keep_block;
@@ -446,6 +478,7 @@ static int batch_configure(mcg_context *ctx, mcg_batch_state *B, mcg_batch_launc
            (tm == MCG_TALLY_GLOBAL ? 0 : (size_t)B->max_cells * 8);
   /* deferral is built for the shared-memory 32-bit tally (the autotuner's
    * candidates); other tally modes run without it */
+  P.defer_lanes = B->defer;
   if (strict && B->defer && tm == MCG_TALLY_SMEM32)
     L.kern = mcg_batch_kernel<true, MCG_TALLY_SMEM32, true>;
   else if (!strict && B->defer && tm == MCG_TALLY_SMEM32)
@@ -713,10 +746,10 @@ extern "C" int mcg_batch_set_launch(mcg_context *ctx, int32_t block, int64_t ite
 
 extern "C" int mcg_batch_set_deferral(mcg_context *ctx, int32_t defer)
 {
-  if (!ctx || (defer != 0 && defer != 1))
+  if (!ctx || defer < 0 || defer > 32)
     return mcg_fail(MCG_ERR_ARG, "mcg_batch_set_deferral: bad arguments");
   mcg_batch_state *B = batch_of(ctx);
-  B->defer = defer != 0;
+  B->defer = defer;
   B->graph_valid = false;
   return MCG_OK;
 }
@@ -741,8 +774,9 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
     return mcg_fail(MCG_ERR_ARG, "mcg_batch_autotune: sample fraction must be in (0, 1]");
   const int blocks[] = {256, 512, 1024};
   const int64_t items[] = {4096, 16384, 65536};
-  /* tally mode and deferral of the full step */
-  const int shapes[][2] = {{MCG_TALLY_SMEM32, 0}, {MCG_TALLY_SMEM32, 1}, {MCG_TALLY_SMEM64, 0}};
+  /* tally mode and deferral of the full step (waiting lanes) */
+  const int shapes[][2] = {{MCG_TALLY_SMEM32, 0}, {MCG_TALLY_SMEM32, 4}, {MCG_TALLY_SMEM32, 8},
+                           {MCG_TALLY_SMEM64, 0}};
   /* every candidate runs the same sample, of at least four times the event
    * engine's drain size (below it the event-based form is a single drain
    * launch, and a persistent launch is dominated by its tail), or the whole
@@ -759,7 +793,7 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
   double best = 1e30; /* ms per history */
   int nc = 0;
   mcg_batch_tuning pick = {B->block, B->tally_mode, B->item_histories, 0.f, 0, MCG_ALGO_HISTORY,
-                           0, B->defer ? 1 : 0};
+                           0, B->defer};
   bool warmed = false;
   for (int64_t it : items) {
     /* the sample keeps the full run's number of items per slab, so the
@@ -772,7 +806,7 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
         const int tm = sh[0];
         B->block = bl;
         B->tally_mode = tm;
-        B->defer = sh[1] != 0;
+        B->defer = sh[1];
         mcg_batch_launch L;
         if ((rc = batch_configure(ctx, B, L)) != MCG_OK)
           return rc;
@@ -809,7 +843,7 @@ extern "C" int mcg_batch_autotune(mcg_context *ctx, double sample_fraction, mcg_
   B->block = pick.block;
   B->tally_mode = pick.tally_mode;
   B->item_histories = pick.item_histories;
-  B->defer = pick.defer != 0;
+  B->defer = pick.defer;
   B->items_built_for = -1;
   B->graph_valid = false;
   pick.candidates = nc;

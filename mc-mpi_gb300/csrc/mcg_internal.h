@@ -29,7 +29,7 @@ struct mcg_batch_state {
   float min_w = 0.f;
   /* launch shape, chosen by mcg_batch_set_launch or the autotuner */
   int block = 512, tally_mode = 1;
-  bool defer = false; /* deferral of the full step (mcg_batch_set_deferral) */
+  int defer = 0; /* waiting lanes of the deferred full step, 0: off (mcg_batch_set_deferral) */
   int64_t item_histories = 16384;
   /* history- or event-based; events per pass of the event engine */
   int algorithm = MCG_ALGO_HISTORY, event_steps = 8;

@@ -61,21 +61,24 @@ def test_batch_strict_matches_oracle(mcg, oracle, small_batch):
 
 @pytest.mark.parametrize("mode", ["strict", "fast"])
 def test_batch_deferral_equals_direct(mcg, small_batch, mode):
-    """Deferring the full step to the end of the refill round changes when a
-    lane's steps run, not what they compute: tallies and counters equal."""
+    """Deferring the full step until enough of a warp's lanes wait for it
+    (1, 8 or 32 waiting lanes, the last only when no other lane can step)
+    changes when a lane's steps run, not what they compute: tallies and
+    counters equal."""
     slabs, sigs, rates = small_batch
     with mcg.Context(mode=mode) as ctx:
         ctx.set_tally_scale(40)
         ctx.batch_set(slabs, sigs, rates, 1e-12)
         ctx.batch_run()
         ref, c_ref = ctx.batch_tally_q(), ctx.counters()
-        ctx.batch_tally_reset()
-        ctx.batch_set_deferral(True)
-        ctx.batch_run()
-        assert np.array_equal(ctx.batch_tally_q(), ref)
-        c = ctx.counters()
-        for key in ("histories", "steps", "scatters", "w_left_q", "w_right_q", "w_killed_q"):
-            assert c[key] == c_ref[key], key
+        for lanes in (1, 8, 32):
+            ctx.batch_tally_reset()
+            ctx.batch_set_deferral(lanes)
+            ctx.batch_run()
+            assert np.array_equal(ctx.batch_tally_q(), ref), lanes
+            c = ctx.counters()
+            for key in ("histories", "steps", "scatters", "w_left_q", "w_right_q", "w_killed_q"):
+                assert c[key] == c_ref[key], (lanes, key)
 
 
 def test_batch_autotune_keeps_parity(mcg, small_batch):
