@@ -532,6 +532,12 @@ __device__ __forceinline__ unsigned long long mcg_globaltimer()
  * reserved by the block's lanes at once, so it never overfills), else to the
  * destination's global ring; idle lanes take from it first. */
 #define MCG_LQ 2048
+
+/* Rounds of the asynchronous workers: steps per lane between two warp
+ * votes, lanes without a particle that end a round, longest round */
+#define MCG_AQ_WINDOW 16
+#define MCG_AQ_ROUND_IDLE 4
+#define MCG_AQ_ROUND_CAP 256
 #define MCG_LQ_BYTES (16 + MCG_LQ * (4 + 4 + (int)sizeof(mcg_particle)))
 
 template <bool STRICT, bool SMEM>
@@ -637,12 +643,14 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
           }
         }
       }
+      /* (the global words below are read only while lanes are still idle:
+       * the block's ring usually serves them all) */
       /* 1. queued particles, when the published count says there are some:
        * each lane looks at one or two rings from this warp's rotating
        * start; the warp tries to claim a run of published tickets from at
        * most four of the non-empty ones */
       long long pend = 0;
-      if (lane == 0)
+      if (lane == 0 && need)
         pend = (long long)mcg_ld_relaxed(reinterpret_cast<unsigned long long *>(pending));
       pend = __shfl_sync(0xffffffffu, pend, 0);
       if (pend > 0) {
@@ -710,7 +718,7 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
        * each, so no ring ever holds more than inflight + the grid's lanes
        * (the capacity the host sizes `inflight` from) */
       unsigned long long sn = 0, dn = 0;
-      if (lane == 0) {
+      if (lane == 0 && need) {
         sn = mcg_ld_relaxed(src_next);
         dn = mcg_ld_relaxed(done);
       }
@@ -782,14 +790,32 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
     sleep_ns = 128;
     int dir = 0;
     bool finished = false;
-    if (active) {
-      const int kmax = (int)min((uint32_t)P.refill_steps, P.max_steps - nst);
-      int k = 0;
-      while ((k < kmax) & (wmc >= min_w) & ((unsigned)(idx - llo) < (unsigned)(lhi - llo))) {
-        mcg_step<STRICT, SMEM ? MCG_TALLY_SMEM32 : MCG_TALLY_GLOBAL>(
-            seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + idx), &tally[idx], qs, T, P.libm);
-        ++k;
+    int k = 0;
+    {
+      /* the round: MCG_AQ_WINDOW steps per lane between two warp votes,
+       * until MCG_AQ_ROUND_IDLE lanes are without a particle to step, one of
+       * them newly (its particle left the sub-domain, ended, or reached the
+       * round's cap), or no lane can step: the queues are visited when
+       * there is something to hand over or to take, not every few steps */
+      const uint32_t kcap = active ? min((uint32_t)MCG_AQ_ROUND_CAP, P.max_steps - nst) : 0u;
+      for (;;) {
+        bool go = ((uint32_t)k < kcap) & (wmc >= min_w) &
+                  ((unsigned)(idx - llo) < (unsigned)(lhi - llo));
+        for (int j = 0; go & (j < MCG_AQ_WINDOW); ++j) {
+          mcg_step<STRICT, SMEM ? MCG_TALLY_SMEM32 : MCG_TALLY_GLOBAL>(
+              seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + idx), &tally[idx], qs, T,
+              P.libm);
+          ++k;
+          go = ((uint32_t)k < kcap) & (wmc >= min_w) &
+               ((unsigned)(idx - llo) < (unsigned)(lhi - llo));
+        }
+        const unsigned gb = __ballot_sync(0xffffffffu, go);
+        const unsigned fb = __ballot_sync(0xffffffffu, active & !go);
+        if (!gb || (fb && __popc(~gb) >= MCG_AQ_ROUND_IDLE))
+          break;
       }
+    }
+    if (active) {
       nst += (uint32_t)k;
       const bool going = (wmc >= min_w) & ((unsigned)(idx - llo) < (unsigned)(lhi - llo));
       if (!going || nst >= P.max_steps) {
