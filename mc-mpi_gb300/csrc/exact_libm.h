@@ -173,6 +173,23 @@ MCG_HD float mcg_exp_small_form(float rh, float rl, float *yl)
   return yh;
 }
 
+/* The small-argument form for rl = 0 without the addition of rl: the same
+ * yh, and yl equal up to the sign of a zero (lo is at most a signed zero
+ * apart, s + lo = s then, and (s - yh) + lo is +0 either way), so |yl| and
+ * every test on it agree with mcg_exp_small_form(t, 0, yl). */
+MCG_HD float mcg_exp_small_yl(float t, float *yl)
+{
+  float p = MCG_FMA(t, MCG_EXP_Q4, MCG_EXP_Q3);
+  p = MCG_FMA(t, p, 0.5f);
+  const float r2 = MCG_MUL(MCG_MUL(t, t), p);
+  const float s = MCG_ADD(1.0f, t);
+  const float se = MCG_SUB(t, MCG_SUB(s, 1.0f));
+  const float lo = MCG_ADD(se, r2);
+  const float yh = MCG_ADD(s, lo);
+  *yl = MCG_ADD(MCG_SUB(s, yh), lo);
+  return yh;
+}
+
 /* Midpoint distance of the small-argument path, in units of 2^-24, the float
  * spacing below 1 (every t < 0); above 1 the spacing is 2^-23 and this
  * measure is only a filter key, which the table generator, running this
