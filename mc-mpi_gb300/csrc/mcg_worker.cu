@@ -109,7 +109,7 @@ __device__ __forceinline__ int mcg_worker_layer_of(const mcg_worker_layer *lay, 
 
 /* One cycle.  SMEM: the chain's tally in shared memory (else global
  * atomics, for chains too long for it). */
-template <bool STRICT, bool SMEM>
+template <bool STRICT, bool SMEM, bool THIN>
 __global__ void __launch_bounds__(1024) mcg_worker_cycle(mcg_worker_params P)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(1024) mcg_worker_cycle(mcg_worker_params P)
           going = false;
           break;
         }
-        mcg_step<STRICT, SMEM ? MCG_TALLY_SMEM32 : MCG_TALLY_GLOBAL>(
+        mcg_step<STRICT, SMEM ? MCG_TALLY_SMEM32 : MCG_TALLY_GLOBAL, THIN>(
             seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + idx), &tally[idx], qs, T, P.libm);
       }
       nst += (uint32_t)k;
@@ -368,8 +368,13 @@ extern "C" int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n
   W.libm = ctx->libm;
   W.libm_tab = ctx->libm_tab;
   W.max_steps = ctx->max_steps;
-  auto kern = strict ? (use_smem ? mcg_worker_cycle<true, true> : mcg_worker_cycle<true, false>)
-                     : (use_smem ? mcg_worker_cycle<false, true> : mcg_worker_cycle<false, false>);
+  /* the strict thin-cell step (mcg_step THIN) on chains where it applies */
+  auto kern = strict ? (ctx->thin ? (use_smem ? mcg_worker_cycle<true, true, true>
+                                              : mcg_worker_cycle<true, false, true>)
+                                  : (use_smem ? mcg_worker_cycle<true, true, false>
+                                              : mcg_worker_cycle<true, false, false>))
+                     : (use_smem ? mcg_worker_cycle<false, true, false>
+                                 : mcg_worker_cycle<false, false, false>);
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin);
   int bps = 1;
   if (e == cudaSuccess)
@@ -540,7 +545,7 @@ __device__ __forceinline__ unsigned long long mcg_globaltimer()
 #define MCG_AQ_ROUND_CAP 256
 #define MCG_LQ_BYTES (16 + MCG_LQ * (4 + 4 + (int)sizeof(mcg_particle)))
 
-template <bool STRICT, bool SMEM>
+template <bool STRICT, bool SMEM, bool THIN>
 __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -802,7 +807,7 @@ __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
         bool go = ((uint32_t)k < kcap) & (wmc >= min_w) &
                   ((unsigned)(idx - llo) < (unsigned)(lhi - llo));
         for (int j = 0; go & (j < MCG_AQ_WINDOW); ++j) {
-          mcg_step<STRICT, SMEM ? MCG_TALLY_SMEM32 : MCG_TALLY_GLOBAL>(
+          mcg_step<STRICT, SMEM ? MCG_TALLY_SMEM32 : MCG_TALLY_GLOBAL, THIN>(
               seed, x, mu, wmc, inv_mu, idx, nsc, __ldg(P.cells + idx), &tally[idx], qs, T,
               P.libm);
           ++k;
@@ -1013,8 +1018,12 @@ extern "C" int mcg_worker_run_async(mcg_context *ctx, const mcg_source *src, int
   /* the launch's deadline: 30 s plus 2 us per history (the benchmark slab
    * runs a history in about 40 ns of GPU time) */
   A.budget_ns = 30000000000ull + 2000ull * (unsigned long long)n;
-  auto kern = strict ? (use_smem ? mcg_worker_async<true, true> : mcg_worker_async<true, false>)
-                     : (use_smem ? mcg_worker_async<false, true> : mcg_worker_async<false, false>);
+  auto kern = strict ? (ctx->thin ? (use_smem ? mcg_worker_async<true, true, true>
+                                              : mcg_worker_async<true, false, true>)
+                                  : (use_smem ? mcg_worker_async<true, true, false>
+                                              : mcg_worker_async<true, false, false>))
+                     : (use_smem ? mcg_worker_async<false, true, false>
+                                 : mcg_worker_async<false, false, false>);
   int bps = 1;
   if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 ctx->smem_optin)) != cudaSuccess ||
