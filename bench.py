@@ -637,6 +637,9 @@ def run_workload(args):
             ctx.set_tally_scale(30)
             ctx.batch_set(slabs, sigs, rates, MIN_W)
             tune = ctx.batch_autotune(0.05)
+            if args.defer >= 0:
+                ctx.batch_set_deferral(args.defer)
+                tune["defer"] = args.defer
             ctx.batch_run()
             ms = []
             for _ in range(args.steps):
@@ -702,6 +705,9 @@ def main():
                     choices=["plain", "batch", "adjoint", "fit", "worker"])
     ap.add_argument("--scale", type=float, default=1.0,
                     help="fraction of the configuration's histories (batch, fit)")
+    ap.add_argument("--defer", type=int, default=-1,
+                    help="batch: waiting lanes of the deferred full step after the autotuner "
+                         "(0 off; default: the autotuner's choice)")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the fast, event, batched, adjoint, worker and fit measurements")
     args = ap.parse_args()

@@ -647,6 +647,10 @@ int mcg_track_launch(mcg_context *ctx, mcg_particle *d_particles, int64_t n, int
     kern = tmode == MCG_TALLY_SMEM64 ? mcg_track_kernel<true, MCG_TALLY_SMEM64, false>
          : tmode == MCG_TALLY_SMEM32 ? mcg_track_kernel<true, MCG_TALLY_SMEM32, false>
                                      : mcg_track_kernel<true, MCG_TALLY_GLOBAL, false>;
+  else if (ctx->thin) /* the fast step ignores THIN but for the loop's unrolling */
+    kern = tmode == MCG_TALLY_SMEM64 ? mcg_track_kernel<false, MCG_TALLY_SMEM64, true>
+         : tmode == MCG_TALLY_SMEM32 ? mcg_track_kernel<false, MCG_TALLY_SMEM32, true>
+                                     : mcg_track_kernel<false, MCG_TALLY_GLOBAL, true>;
   else
     kern = tmode == MCG_TALLY_SMEM64 ? mcg_track_kernel<false, MCG_TALLY_SMEM64, false>
          : tmode == MCG_TALLY_SMEM32 ? mcg_track_kernel<false, MCG_TALLY_SMEM32, false>

@@ -515,6 +515,9 @@ __device__ __forceinline__ void mcg_step_rest(uint64_t &seed, float &x, float &m
   idx = inew;
 }
 
+/* THIN: the chain is optically thin (every |sig_a cell width| <= 5e-4):
+ * the strict step's thin certain-crossing path, and, in both arithmetics,
+ * four steps per pass of the step loop. */
 template <bool STRICT, int TALLY, bool THIN>
 __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
 {
@@ -599,8 +602,11 @@ __global__ void __launch_bounds__(1024) mcg_track_kernel(mcg_track_params P)
        * range test of simulate_particle's loop */
       const int kmax = (int)min((uint32_t)P.refill_steps, P.max_steps - nst);
       int k = 0;
-      /* four steps per loop pass: measured 3 % faster (strict) than one */
-#pragma unroll 4
+      /* four steps per loop pass on thin chains: measured 3 % faster
+       * (strict) than one; on thicker chains, where crossings split between
+       * the exp evaluator's paths, one (four measured 36 % slower) */
+      constexpr int kUnroll = THIN ? 4 : 1;
+#pragma unroll kUnroll
       for (; k < kmax;) {
         if (!((wmc >= min_w) & ((unsigned)idx < (unsigned)ncell)))
           break;
