@@ -363,7 +363,12 @@ def run_gpu(args):
                                                    ctx.conversion_rates()),
         "issue_roofline": {"bound": "issue", "n_alg_ops_per_step": n_alg,
                            "achieved_gops": (counters["steps"] / dev_s) * n_alg / 1e9,
-                           "peak_gops": sms * 128 * f_sm / 1e9, "frac": issue_frac},
+                           "peak_gops": sms * 128 * f_sm / 1e9, "frac": issue_frac,
+                           # the step's two algorithmic transcendentals (log, exp) against
+                           # 16 special-function results per SM per clock
+                           "mufu_alg_per_step": 2,
+                           "mufu_frac": (counters["steps"] / dev_s) * 2 / (sms * 16 * f_sm)
+                           if steps_per_s else None},
         "clocks": clocks,
     }
     if rank == 0 and not args.no_extra:
