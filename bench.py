@@ -454,9 +454,25 @@ def bench_batched(mcg, mode, device, scale=1.0, reps=2):
         ctx.batch_run_per_slab()
         ms_plain = ctx.last_kernel_ms()
         same = bool(np.array_equal(ctx.batch_tally_q(), q_batch))
+    fast_ms = None
+    if mode == "strict":
+        # the same histories with the fast arithmetic, in the strict run's
+        # launch shape (statistically equivalent tallies)
+        with mcg.Context(mode="fast", device=device) as fctx:
+            fctx.set_tally_scale(30)
+            fctx.batch_set(slabs, sigs, rates, MIN_W)
+            fctx.batch_set_launch(tune["block"], tune["item_histories"], tune["tally_mode"])
+            fctx.batch_set_deferral(tune["defer"])
+            if tune["algorithm"] == 1:
+                fctx.batch_set_algorithm("event", tune["steps_per_pass"])
+            fctx.batch_run()
+            fctx.batch_tally_reset()
+            fctx.batch_run()
+            fast_ms = fctx.last_kernel_ms()
     t = min(ms) / 1e3
     return {"value": n / t, "unit": "histories/s", "per_slab_value": n / (ms_plain / 1e3),
             "speedup_vs_per_slab": (ms_plain / 1e3) / t, "identical_tallies": same,
+            "fast_value": None if fast_ms is None else n / (fast_ms / 1e3),
             "steps_per_s": steps / t, "histories": n, "launches": 1, "autotuned": tune,
             "workload": f"4096 slabs, cells U{{16..4096}}, L~U[0.5,5], sigma_a~U[0.1,5], "
                         f"sigma_s~U[0,10], histories log-uniform [1e3,1e6] x {scale}",
