@@ -13,7 +13,9 @@
  * histories of different lengths; the block synchronises only between
  * items.  The per-cell step table of every slab lives in HBM (16 B per cell)
  * and is read through L1.  The step is mcg_step (mcg_track.cuh), i.e.
- * Layer::particle_step of src/layer.cpp:123-190.
+ * Layer::particle_step of src/layer.cpp:123-190; with deferral on, it is
+ * split into the certain crossing (mcg_step_cross) and the rest of the step
+ * (mcg_step_rest), which a warp runs for its waiting lanes together.
  */
 #include <algorithm>
 #include <new>
