@@ -69,6 +69,16 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
   long long *s_ctl = reinterpret_cast<long long *>(s_cnt + 16); /* item, local history counter */
   unsigned long long *s_tally = reinterpret_cast<unsigned long long *>(s_ctl + 4);
   const int tid = threadIdx.x, lane = tid & 31;
+  /* r-step jumps of the seed chain, s -> (A_r s + C_r) mod 2^63 for
+   * r < 32: a warp finds the chain state of the first history of each
+   * 32-history chunk it takes with one jump-ahead, run by all its lanes
+   * together, and each lane its own from there with one multiply-add */
+  __shared__ unsigned long long s_jump[64];
+  if (tid < 32) {
+    const uint64_t c = mcg_lcg_skip(0ull, (uint64_t)tid, 1);
+    s_jump[tid] = (mcg_lcg_skip(1ull, (uint64_t)tid, 1) - c) & MCG_MASK63;
+    s_jump[32 + tid] = c;
+  }
   if (STRICT) {
     const float *src = reinterpret_cast<const float *>(P.libm_tab);
     float *dst = reinterpret_cast<float *>(T);
@@ -123,12 +133,17 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
     bool active = false;
     bool wait = false; /* DEFER: the lane's step waits for the full step */
     long long pool_next = 0, pool_end = 0;
+    /* the chunk the pool lies in: its first history and that history's
+     * seed-chain state (seed_mode 0) */
+    long long pool_base = 0;
+    uint64_t pool_seed = 0;
     bool drained = false;
     for (;;) {
       unsigned need = __ballot_sync(0xffffffffu, !active);
       if (need) {
         int cnt = __popc(need), rank = __popc(need & lanemask_lt());
-        long long avail = pool_end - pool_next, my = -1;
+        long long avail = pool_end - pool_next, my = -1, my_base = pool_base;
+        uint64_t my_seed = pool_seed;
         if (rank < avail)
           my = pool_next + rank;
         if (cnt > avail && !drained) {
@@ -142,8 +157,14 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
           } else {
             long long end = min(base + 32, (long long)it.count);
             long long r2 = rank - avail;
-            if (rank >= avail && r2 < end - base)
+            pool_base = base;
+            if (S.seed_mode == 0)
+              pool_seed = mcg_lcg_skip(S.base_seed, (uint64_t)(it.first + base) + 1, 1);
+            if (rank >= avail && r2 < end - base) {
               my = base + r2;
+              my_base = base;
+              my_seed = pool_seed;
+            }
             pool_next = min(base + (cnt - avail), end);
             pool_end = end;
           }
@@ -151,7 +172,13 @@ __global__ void __launch_bounds__(1024) mcg_batch_kernel(mcg_batch_params P)
           pool_next += min((long long)cnt, avail);
         }
         if (!active && my >= 0) {
-          mcg_source_particle(S, it.first + my, seed, x, mu, wmc, idx);
+          if (S.seed_mode == 0) {
+            const int r = (int)(my - my_base); /* 0 <= r < 32: my lies in its chunk */
+            mcg_source_particle_at(S, (s_jump[r] * my_seed + s_jump[32 + r]) & MCG_MASK63, seed, x,
+                                   mu, wmc, idx);
+          } else {
+            mcg_source_particle(S, it.first + my, seed, x, mu, wmc, idx);
+          }
           inv_mu = mcg_flight_rcp(mu);
           wres = 0.f;
           nst = nsc = 0;

@@ -310,12 +310,11 @@ __device__ __forceinline__ float mcg_flight_log2(uint64_t s)
   return u < 0x1p-8f ? near1 : __log2f(__fmaf_rn(__uint2float_rn(t), 0x1p-32f, 0x1p-33f));
 }
 
-/* 1 - e^t for |t| < 2^-7: -t (1 + t/2 + t^2/6 + t^3/24), truncation below
- * 2^-31 relative. */
+/* 1 - e^t for |t| < 2^-7: -t (1 + t/2 + t^2/6), truncation below
+ * |t|^3/24 < 2^-25.5 relative, under the rounding of the float result. */
 __device__ __forceinline__ float mcg_one_minus_exp_small(float t)
 {
-  float p = fmaf(t, 1.0f / 24.0f, 1.0f / 6.0f);
-  p = fmaf(t, p, 0.5f);
+  float p = fmaf(t, 1.0f / 6.0f, 0.5f);
   p = fmaf(t, p, 1.0f);
   return -t * p;
 }

@@ -103,12 +103,13 @@ __device__ __forceinline__ void mcg_deposit(unsigned long long *t, float dw, int
 enum { MCG_CNT_HIST = 0, MCG_CNT_STEPS, MCG_CNT_SCAT, MCG_CNT_LEFT, MCG_CNT_RIGHT, MCG_CNT_KILL,
        MCG_CNT_WLEFT, MCG_CNT_WRIGHT, MCG_CNT_WKILL, MCG_CNT_ERR, MCG_CNT_N };
 
-/* Particle k of a device-born source (see mcg_source in mcgb300.h). */
-__device__ __forceinline__ void mcg_source_particle(const mcg_source &S, int64_t k, uint64_t &seed,
-                                                    float &x, float &mu, float &wmc, int &idx)
+/* Particle of a device-born source (see mcg_source in mcgb300.h) whose
+ * seed-chain state s is known: particle k has s = the chain's (k+1)-th
+ * state from base_seed (seed_mode 0) or base_seed + k (seed_mode 1). */
+__device__ __forceinline__ void mcg_source_particle_at(const mcg_source &S, uint64_t s,
+                                                       uint64_t &seed, float &x, float &mu,
+                                                       float &wmc, int &idx)
 {
-  uint64_t s = S.seed_mode == 0 ? mcg_lcg_skip(S.base_seed, (uint64_t)k + 1, 1)
-                                : ((S.base_seed + (uint64_t)k) & MCG_MASK63);
   float m = S.mu0;
   if (S.isotropic == 1)
     m = __fsub_rn(__fmul_rn(2.0f, mcg_rnd_real(s)), 1.0f);
@@ -119,6 +120,15 @@ __device__ __forceinline__ void mcg_source_particle(const mcg_source &S, int64_t
   mu = m;
   wmc = S.w0;
   idx = S.cell0;
+}
+
+/* Particle k of a device-born source. */
+__device__ __forceinline__ void mcg_source_particle(const mcg_source &S, int64_t k, uint64_t &seed,
+                                                    float &x, float &mu, float &wmc, int &idx)
+{
+  const uint64_t s = S.seed_mode == 0 ? mcg_lcg_skip(S.base_seed, (uint64_t)k + 1, 1)
+                                      : ((S.base_seed + (uint64_t)k) & MCG_MASK63);
+  mcg_source_particle_at(S, s, seed, x, mu, wmc, idx);
 }
 
 __device__ __forceinline__ void mcg_load_particle(const mcg_track_params &P, int64_t i,
