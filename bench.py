@@ -212,7 +212,15 @@ def run_reference(args):
         "config": {"workload": WORKLOAD,
                    "batch": per_step, "l2": "n/a (host)"},
         "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port",
-                         "sample": f"{per_step} histories per step"},
+                         "sample": f"{per_step} histories per step of the same 1e8-history "
+                                   "source (consecutive indices from 3e6), sized to about four "
+                                   "seconds of host work per step; the GPU arm runs all 1e8 "
+                                   "per step",
+                         "note": "the oracle's restatement of Layer::simulate (bit-exact with "
+                                 "the reference's compiled Layer; its speed measured at 0.98x "
+                                 "of it single-threaded), OpenMP over all host cores: the "
+                                 "reference's own intra-rank parallelism, mpirun being "
+                                 "unavailable on this box"},
         "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
