@@ -537,13 +537,13 @@ __device__ __forceinline__ unsigned long long mcg_globaltimer()
  * reserved by the block's lanes at once, so it never overfills), else to the
  * destination's global ring; idle lanes take from it first. */
 #define MCG_LQ 2048
+#define MCG_LQ_BYTES (16 + MCG_LQ * (4 + 4 + (int)sizeof(mcg_particle)))
 
 /* Rounds of the asynchronous workers: steps per lane between two warp
  * votes, lanes without a particle that end a round, longest round */
 #define MCG_AQ_WINDOW 16
 #define MCG_AQ_ROUND_IDLE 4
 #define MCG_AQ_ROUND_CAP 256
-#define MCG_LQ_BYTES (16 + MCG_LQ * (4 + 4 + (int)sizeof(mcg_particle)))
 
 template <bool STRICT, bool SMEM, bool THIN>
 __global__ void __launch_bounds__(1024) mcg_worker_async(mcg_async_params P)
