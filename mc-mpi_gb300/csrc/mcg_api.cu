@@ -639,7 +639,7 @@ int mcg_track_launch(mcg_context *ctx, mcg_particle *d_particles, int64_t n, int
   size_t smem = base + (tmode == MCG_TALLY_GLOBAL ? 0 : (size_t)ctx->n_cells * 8 * copies);
   P.tally_copies = copies;
   void (*kern)(mcg_track_params);
-  if (strict && ctx->thin)
+  if (strict && mcg_strict_thin(ctx))
     kern = tmode == MCG_TALLY_SMEM64 ? mcg_track_kernel<true, MCG_TALLY_SMEM64, true>
          : tmode == MCG_TALLY_SMEM32 ? mcg_track_kernel<true, MCG_TALLY_SMEM32, true>
                                      : mcg_track_kernel<true, MCG_TALLY_GLOBAL, true>;

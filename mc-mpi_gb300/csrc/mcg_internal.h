@@ -161,6 +161,14 @@ inline unsigned long long mcg_event_drain_below(const mcg_context *ctx)
 {
   return (unsigned long long)ctx->sm_count * 1024;
 }
+/* The strict thin-cell step applies: a thin chain, and exception-table
+ * thresholds small enough for its test on |yl| (that test implies the
+ * midpoint-distance test for thresholds below 0.4; the tables' are about
+ * 0.002). */
+inline bool mcg_strict_thin(const mcg_context *ctx)
+{
+  return ctx->thin && ctx->libm.tau_exp_max < 0.25f;
+}
 int mcg_event_run(mcg_context *ctx, mcg_track_params &P);
 int mcg_event_run_slabs(mcg_context *ctx, const float4 *cells, unsigned long long *tally,
                         const void *slabs, const unsigned long long *slab_hist0, int n_slabs,

@@ -228,9 +228,10 @@ __device__ __forceinline__ void mcg_step(uint64_t &seed, float &x, float &mu, fl
      * above the table's largest threshold tau; the thin form tests |yl|
      * against (0.5 - tau) 2^-24 (1 - 2^-21) instead, which implies it: the
      * bound's two roundings leave it below (0.5 - tau) 2^-24 (1 - 3.5e-7),
-     * so 0.5 - |yl| 2^24 exceeds tau by more than 1.7e-7 (tau < 0.01),
-     * more than the 2^-25 rounding of that subtraction; two operations
-     * less per step */
+     * so 0.5 - |yl| 2^24 exceeds tau by more than 3.5e-8 for tau < 0.4,
+     * more than the 2^-25 rounding of that subtraction (the host takes this
+     * form only for tables with tau < 0.25, mcg_strict_thin); two
+     * operations less per step */
     float d_q = 0.f, yl_q = 0.f;
     const float y_q = THIN ? mcg_exp_small_yl(t_q, &yl_q) : mcg_exp_ff_core(t_q, &d_q, T);
     const bool far_q =

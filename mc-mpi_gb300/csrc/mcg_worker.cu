@@ -369,7 +369,7 @@ extern "C" int mcg_worker_run(mcg_context *ctx, const mcg_source *src, int64_t n
   W.libm_tab = ctx->libm_tab;
   W.max_steps = ctx->max_steps;
   /* the strict thin-cell step (mcg_step THIN) on chains where it applies */
-  auto kern = strict ? (ctx->thin ? (use_smem ? mcg_worker_cycle<true, true, true>
+  auto kern = strict ? (mcg_strict_thin(ctx) ? (use_smem ? mcg_worker_cycle<true, true, true>
                                               : mcg_worker_cycle<true, false, true>)
                                   : (use_smem ? mcg_worker_cycle<true, true, false>
                                               : mcg_worker_cycle<true, false, false>))
@@ -1018,7 +1018,7 @@ extern "C" int mcg_worker_run_async(mcg_context *ctx, const mcg_source *src, int
   /* the launch's deadline: 30 s plus 2 us per history (the benchmark slab
    * runs a history in about 40 ns of GPU time) */
   A.budget_ns = 30000000000ull + 2000ull * (unsigned long long)n;
-  auto kern = strict ? (ctx->thin ? (use_smem ? mcg_worker_async<true, true, true>
+  auto kern = strict ? (mcg_strict_thin(ctx) ? (use_smem ? mcg_worker_async<true, true, true>
                                               : mcg_worker_async<true, false, true>)
                                   : (use_smem ? mcg_worker_async<true, true, false>
                                               : mcg_worker_async<true, false, false>))
