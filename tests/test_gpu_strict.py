@@ -398,6 +398,27 @@ def test_async_worker_matches_fused(mcg, mode):
         assert np.array_equal(ctx.tally_q(), fused)
 
 
+@pytest.mark.parametrize("mode", ["strict", "fast"])
+def test_workers_on_a_thick_chain_match_fused(mcg, mode):
+    """Both worker forms on a chain too thick for the thin-cell step (1000
+    cells on [0, 2], sigma_a up to 4 per unit, 8 sub-domains: the strict
+    full-exp instances) give the fused tracker's tallies exactly."""
+    from mc_mpi_gb300 import workloads
+    sig_a, sig_s, _ = workloads.config3()
+    sigs, rates = workloads.sigs_rates(sig_a, sig_s)
+    st, m, dx, _, _ = mcg.layer_decomposition(0.0, 1.0, 1000, 8)
+    with mcg.Context(mode=mode) as ctx:
+        ctx.set_layers(st, m, dx, sigs, rates, 1e-12)
+        ctx.simulate_source(0, 5000)
+        fused = ctx.tally_q()
+        ctx.tally_reset()
+        ctx.worker_run_async(5000)
+        assert np.array_equal(ctx.tally_q(), fused)
+        ctx.tally_reset()
+        ctx.worker_run(5000, per_cycle=1000, queue_capacity=1 << 14)
+        assert np.array_equal(ctx.tally_q(), fused)
+
+
 def test_worker_matches_reference_workersync_tally(mcg):
     """Against the reference's own Layer::simulate driven by the WorkerSync
     cycle (golden fixture): float tallies agree to float accuracy."""
