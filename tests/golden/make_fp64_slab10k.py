@@ -18,7 +18,7 @@ written each time the count reaches one of the requested sizes:
     python tests/golden/make_fp64_slab10k.py 10000000 100000000
 
 writes fp64_slab10k_1e7.npz after 1e7 histories and fp64_slab10k_1e8.npz
-after 1e8 (about 73 minutes on 8 x86 cores).  The fixture does not depend on
+after 1e8 (about 55 minutes on 8 x86 cores).  The fixture does not depend on
 the host C library beyond double-precision rounding, so it serves the GPU
 box, where the statistical tests of the fast arithmetic read it.
 """
